@@ -1,0 +1,735 @@
+// C ABI of the GB300 advection operator (include/advection_gb300.h).
+//
+// Host side of AdvectionOperation (advection_solver.cc:329-818) and
+// LowStorageRungeKuttaIntegrator (advection_solver.cc:822-944): set-up of
+// mesh, tables and geometry on the device, and the stage sequencing with the
+// buffer rotation that lets every fused stage kernel read r_in while writing
+// its outputs to other buffers.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/advection_gb300.h"
+#include "geometry.h"
+#include "kernels.h"
+#include "tables.h"
+
+struct adv_handle
+{
+  adv_config       cfg;
+  adv::Mesh        mesh;
+  adv::Tables1D    tb;
+  int              device = 0;
+  double           h_min  = 0.0;
+  // uniform-case constants
+  double cv[3] = {}, P[3] = {}, M[3] = {};
+  // device buffers
+  void    *d_cell_geo    = nullptr;
+  void    *d_face_geo[3] = {};
+  double  *d_face_x[3]   = {};
+  double  *d_partials    = nullptr;
+  double  *d_scratch[2]  = {};
+  int64_t  device_bytes  = 0;
+  int64_t  launches      = 0;
+  adv::DiagArgs diag;
+};
+
+namespace
+{
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg)
+{
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *where)
+{
+  g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? ADV_ERR_OUT_OF_MEMORY : ADV_ERR_CUDA;
+}
+
+#define ADV_CUDA(call)                               \
+  do                                                 \
+    {                                                \
+      cudaError_t e_ = (call);                       \
+      if (e_ != cudaSuccess)                         \
+        return cuda_fail(e_, #call);                 \
+    }                                                \
+  while (0)
+
+std::mutex g_table_mutex;
+bool       g_tables_uploaded[256] = {};
+
+int ensure_tables(int device)
+{
+  std::lock_guard<std::mutex> lock(g_table_mutex);
+  if (device < 0 || device >= 256)
+    return fail(ADV_ERR_INVALID, "device index out of range");
+  if (g_tables_uploaded[device])
+    return ADV_OK;
+  static adv::DevTables<double> td[adv::kMaxNDev + 1];
+  static adv::DevTables<float>  tf[adv::kMaxNDev + 1];
+  std::memset(td, 0, sizeof(td));
+  std::memset(tf, 0, sizeof(tf));
+  for (int n = 2; n <= adv::kMaxNDev; ++n)
+    {
+      adv::Tables1D t;
+      t.init(n - 1);
+      for (int q = 0; q < n; ++q)
+        {
+          for (int i = 0; i < n; ++i)
+            {
+              td[n].S[q][i]  = t.S[q][i];
+              td[n].Si[q][i] = t.Si[q][i];
+              td[n].Dw[q][i] = t.Dw[q][i];
+              td[n].D[q][i]  = t.D[q][i];
+              tf[n].S[q][i]  = (float)t.S[q][i];
+              tf[n].Si[q][i] = (float)t.Si[q][i];
+              tf[n].Dw[q][i] = (float)t.Dw[q][i];
+              tf[n].D[q][i]  = (float)t.D[q][i];
+            }
+          td[n].l0[q] = t.l0[q], td[n].l1[q] = t.l1[q];
+          td[n].lw0[q] = t.lw0[q], td[n].lw1[q] = t.lw1[q], td[n].gw[q] = t.gw[q];
+          tf[n].l0[q] = (float)t.l0[q], tf[n].l1[q] = (float)t.l1[q];
+          tf[n].lw0[q] = (float)t.lw0[q], tf[n].lw1[q] = (float)t.lw1[q], tf[n].gw[q] = (float)t.gw[q];
+        }
+    }
+  ADV_CUDA(adv::upload_tables_stage64(td, tf));
+  ADV_CUDA(adv::upload_tables_stage32(td, tf));
+  ADV_CUDA(adv::upload_tables_diag(td, tf));
+  g_tables_uploaded[device] = true;
+  return ADV_OK;
+}
+
+int validate(const adv_config &c)
+{
+  if (c.degree < 1 || c.degree > 6)
+    return fail(ADV_ERR_INVALID, "degree must be in 1..6");
+  for (int d = 0; d < 3; ++d)
+    {
+      if (c.n_cells[d] < 1)
+        return fail(ADV_ERR_INVALID, "n_cells must be >= 1 in every direction");
+      if (!(c.domain_hi[d] > c.domain_lo[d]))
+        return fail(ADV_ERR_INVALID, "domain_hi must exceed domain_lo");
+    }
+  const double nc = (double)c.n_cells[0] * c.n_cells[1] * c.n_cells[2];
+  if (nc * std::pow(c.degree + 1.0, 3) > 2.0e9)
+    return fail(ADV_ERR_INVALID, "more than 2e9 degrees of freedom are not supported");
+  if (nc > 2.0e9)
+    return fail(ADV_ERR_INVALID, "too many cells");
+  if (c.mesh_type != ADV_MESH_CARTESIAN && c.mesh_type != ADV_MESH_DEFORMED)
+    return fail(ADV_ERR_INVALID, "unknown mesh_type");
+  if (c.mesh_type == ADV_MESH_DEFORMED && !(std::fabs(c.deformation) < 0.1))
+    return fail(ADV_ERR_INVALID, "|deformation| must be below 0.1 to keep the mapping invertible");
+  if (c.velocity_type != ADV_VELOCITY_CONSTANT && c.velocity_type != ADV_VELOCITY_ROTATING)
+    return fail(ADV_ERR_INVALID, "unknown velocity_type");
+  if (c.velocity_type == ADV_VELOCITY_ROTATING && !(c.velocity_period > 0.0))
+    return fail(ADV_ERR_INVALID, "velocity_period must be positive for the rotating field");
+  if (c.initial_condition < ADV_IC_SINE_GAUSS || c.initial_condition > ADV_IC_WAVE)
+    return fail(ADV_ERR_INVALID, "unknown initial_condition");
+  if (c.initial_condition == ADV_IC_BLOB && !(c.ic_params[3] > 0.0))
+    return fail(ADV_ERR_INVALID, "blob width ic_params[3] must be positive");
+  if (c.precision != ADV_PRECISION_FP64 && c.precision != ADV_PRECISION_FP32_OPERATOR)
+    return fail(ADV_ERR_INVALID, "unknown precision");
+  if (c.diffusion != 0.0)
+    return fail(ADV_ERR_INVALID, "diffusion (SIPG) is not available in this build");
+  if (!(c.flux_alpha >= 0.0 && c.flux_alpha <= 1.0))
+    return fail(ADV_ERR_INVALID, "flux_alpha must be in [0, 1]");
+  return ADV_OK;
+}
+
+template <typename T>
+int upload_array(const std::vector<double> &src, void **dst, int64_t &bytes)
+{
+  std::vector<T> tmp(src.begin(), src.end());
+  const size_t   nb = tmp.size() * sizeof(T);
+  ADV_CUDA(cudaMalloc(dst, nb));
+  ADV_CUDA(cudaMemcpy(*dst, tmp.data(), nb, cudaMemcpyHostToDevice));
+  bytes += (int64_t)nb;
+  return ADV_OK;
+}
+
+void fill_diag(adv_handle &h)
+{
+  adv::DiagArgs &g = h.diag;
+  std::memset(&g, 0, sizeof(g));
+  const adv::Mesh &m = h.mesh;
+  const int        n = m.n;
+  g.n                = n;
+  for (int d = 0; d < 3; ++d)
+    {
+      g.nc[d] = m.nc[d];
+      g.lo[d] = m.lo[d];
+      g.L[d]  = m.L[d];
+      g.h[d]  = m.h[d];
+    }
+  g.n_cells     = m.n_cells;
+  g.curved      = m.curved;
+  g.deformation = h.cfg.deformation;
+  g.ex.type     = h.cfg.initial_condition;
+  g.ex.constant_velocity = h.cfg.velocity_type == ADV_VELOCITY_CONSTANT;
+  for (int d = 0; d < 3; ++d)
+    {
+      g.ex.velocity[d] = h.cfg.velocity[d];
+      g.ex.lo[d]       = m.lo[d];
+      g.ex.L[d]        = m.L[d];
+    }
+  for (int i = 0; i < 8; ++i)
+    g.ex.p[i] = h.cfg.ic_params[i];
+  for (int i = 0; i < n; ++i)
+    g.gl[i] = h.tb.gl[i], g.gp[i] = h.tb.gp[i], g.gw[i] = h.tb.gw[i];
+  adv::gauss_points(n + 1, g.ep, g.ew);
+  for (int q = 0; q < n; ++q)
+    for (int i = 0; i < n; ++i)
+      {
+        g.S[q * n + i]  = h.tb.S[q][i];
+        g.Sd[q * n + i] = h.tb.Sd[q][i];
+        g.Si[q * n + i] = h.tb.Si[q][i];
+      }
+  for (int p = 0; p < n + 1; ++p)
+    for (int i = 0; i < n; ++i)
+      {
+        g.SE[p * n + i]  = adv::lagrange(h.tb.gl, n, i, g.ep[p]);
+        g.SEd[p * n + i] = adv::lagrange_derivative(h.tb.gl, n, i, g.ep[p]);
+      }
+}
+
+// velocity time factor of the rotating field at time t (1 for a constant velocity)
+double time_factor(const adv_handle &h, double t)
+{
+  if (h.cfg.velocity_type == ADV_VELOCITY_CONSTANT)
+    return 1.0;
+  return std::cos(3.14159265358979323846 * t / h.cfg.velocity_period);
+}
+
+adv::StageArgs base_args(const adv_handle &h, double t)
+{
+  adv::StageArgs A;
+  std::memset(&A, 0, sizeof(A));
+  const adv::Mesh &m = h.mesh;
+  for (int d = 0; d < 3; ++d)
+    {
+      A.nc[d]   = m.nc[d];
+      A.npos[d] = m.npos[d];
+      A.cv[d]   = h.cv[d];
+      A.P[d]    = h.P[d];
+      A.M[d]    = h.M[d];
+      A.cvf[d]  = (float)h.cv[d];
+      A.Pf[d]   = (float)h.P[d];
+      A.Mf[d]   = (float)h.M[d];
+      A.face_geo[d] = h.d_face_geo[d];
+      A.face_x[d]   = h.d_face_x[d];
+    }
+  A.n_cells  = m.n_cells;
+  A.periodic = m.periodic;
+  A.uniform  = m.uniform;
+  A.bc_exact = h.cfg.boundary_value == ADV_BOUNDARY_EXACT;
+  A.skew     = h.cfg.factor_skew;
+  A.skewf    = (float)h.cfg.factor_skew;
+  A.has_skew = h.cfg.factor_skew != 0.0;
+  A.cell_geo = h.d_cell_geo;
+  A.t        = t;
+  A.ex       = h.diag.ex;
+  const double s = time_factor(h, t);
+  A.swap_pm      = s < 0.0;
+  A.out_scale    = s;
+  return A;
+}
+
+int launch(adv_handle *h, const adv::StageArgs &A, cudaStream_t s)
+{
+  cudaError_t e = h->cfg.precision == ADV_PRECISION_FP64 ? adv::launch_stage_fp64(h->mesh.n, A, s)
+                                                           : adv::launch_stage_fp32(h->mesh.n, A, s);
+  if (e != cudaSuccess)
+    return cuda_fail(e, "stage kernel launch");
+  ++h->launches;
+  return ADV_OK;
+}
+
+int ensure_scratch(adv_handle *h, int i)
+{
+  if (!h->d_scratch[i])
+    {
+      ADV_CUDA(cudaMalloc(&h->d_scratch[i], h->mesh.n_dofs * sizeof(double)));
+      h->device_bytes += h->mesh.n_dofs * sizeof(double);
+    }
+  return ADV_OK;
+}
+
+int check_device(const adv_handle *h)
+{
+  int dev = -1;
+  ADV_CUDA(cudaGetDevice(&dev));
+  if (dev != h->device)
+    return fail(ADV_ERR_INVALID, "handle was created on another device than the current one");
+  return ADV_OK;
+}
+} // namespace
+
+extern "C" {
+
+void adv_config_default(adv_config *c)
+{
+  std::memset(c, 0, sizeof(*c));
+  c->degree = 3;
+  for (int d = 0; d < 3; ++d)
+    {
+      c->n_cells[d]   = 8;
+      c->domain_lo[d] = 0.0;
+      c->domain_hi[d] = 1.0;
+    }
+  c->mesh_type         = ADV_MESH_CARTESIAN;
+  c->periodic          = 1;
+  c->velocity_type     = ADV_VELOCITY_CONSTANT;
+  c->initial_condition = ADV_IC_SINE_GAUSS;
+  c->velocity[0]       = 1.0;
+  c->velocity[1]       = 0.15;
+  c->velocity[2]       = -0.05;
+  c->velocity_period   = 1.0;
+  c->flux_alpha        = 1.0;
+  c->penalty_factor    = 1.0;
+  c->boundary_value    = ADV_BOUNDARY_EXACT;
+  c->precision         = ADV_PRECISION_FP64;
+}
+
+const char *adv_last_error(void) { return g_last_error.c_str(); }
+
+int adv_create(const adv_config *cfg, adv_handle **out)
+{
+  if (!cfg || !out)
+    return fail(ADV_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (int e = validate(*cfg))
+    return e;
+  auto *h = new adv_handle();
+  h->cfg  = *cfg;
+  int rc  = ADV_OK;
+  do
+    {
+      cudaError_t e = cudaGetDevice(&h->device);
+      if (e != cudaSuccess)
+        {
+          rc = cuda_fail(e, "cudaGetDevice");
+          break;
+        }
+      if ((rc = ensure_tables(h->device)))
+        break;
+      adv::setup_mesh(h->cfg, h->mesh);
+      h->tb.init(h->cfg.degree);
+      adv::HostGeometry g;
+      adv::compute_geometry(h->cfg, h->mesh, h->tb, g);
+      h->h_min = g.h_min;
+      for (int d = 0; d < 3; ++d)
+        h->cv[d] = g.cv[d], h->P[d] = g.P[d], h->M[d] = g.M[d];
+      const bool fp64 = h->cfg.precision == ADV_PRECISION_FP64;
+      if (!g.cell.empty())
+        rc = fp64 ? upload_array<double>(g.cell, &h->d_cell_geo, h->device_bytes)
+                  : upload_array<float>(g.cell, &h->d_cell_geo, h->device_bytes);
+      for (int d = 0; d < 3 && rc == ADV_OK; ++d)
+        {
+          if (!g.face[d].empty())
+            rc = fp64 ? upload_array<double>(g.face[d], &h->d_face_geo[d], h->device_bytes)
+                      : upload_array<float>(g.face[d], &h->d_face_geo[d], h->device_bytes);
+          if (rc == ADV_OK && !g.face_x[d].empty())
+            rc = upload_array<double>(g.face_x[d], (void **)&h->d_face_x[d], h->device_bytes);
+        }
+      if (rc)
+        break;
+      e = cudaMalloc(&h->d_partials, 3 * 4096 * sizeof(double));
+      if (e != cudaSuccess)
+        {
+          rc = cuda_fail(e, "cudaMalloc partials");
+          break;
+        }
+      h->device_bytes += 3 * 4096 * sizeof(double);
+      fill_diag(*h);
+    }
+  while (false);
+  if (rc)
+    {
+      adv_destroy(h);
+      return rc;
+    }
+  *out = h;
+  return ADV_OK;
+}
+
+int adv_destroy(adv_handle *h)
+{
+  if (!h)
+    return ADV_OK;
+  cudaFree(h->d_cell_geo);
+  for (int d = 0; d < 3; ++d)
+    {
+      cudaFree(h->d_face_geo[d]);
+      cudaFree(h->d_face_x[d]);
+    }
+  cudaFree(h->d_partials);
+  cudaFree(h->d_scratch[0]);
+  cudaFree(h->d_scratch[1]);
+  delete h;
+  return ADV_OK;
+}
+
+int adv_n_dofs(const adv_handle *h, int64_t *out)
+{
+  if (!h || !out)
+    return fail(ADV_ERR_INVALID, "null argument");
+  *out = h->mesh.n_dofs;
+  return ADV_OK;
+}
+
+int adv_n_cells(const adv_handle *h, int64_t *out)
+{
+  if (!h || !out)
+    return fail(ADV_ERR_INVALID, "null argument");
+  *out = h->mesh.n_cells;
+  return ADV_OK;
+}
+
+int adv_device_bytes(const adv_handle *h, int64_t *out)
+{
+  if (!h || !out)
+    return fail(ADV_ERR_INVALID, "null argument");
+  *out = h->device_bytes;
+  return ADV_OK;
+}
+
+int adv_launch_count(const adv_handle *h, int64_t *out)
+{
+  if (!h || !out)
+    return fail(ADV_ERR_INVALID, "null argument");
+  *out = h->launches;
+  return ADV_OK;
+}
+
+int adv_alloc_vector(adv_handle *h, double **out)
+{
+  if (!h || !out)
+    return fail(ADV_ERR_INVALID, "null argument");
+  ADV_CUDA(cudaMalloc(out, h->mesh.n_dofs * sizeof(double)));
+  ADV_CUDA(cudaMemset(*out, 0, h->mesh.n_dofs * sizeof(double)));
+  return ADV_OK;
+}
+
+int adv_free_vector(adv_handle *h, double *vec)
+{
+  if (!h)
+    return fail(ADV_ERR_INVALID, "null handle");
+  ADV_CUDA(cudaFree(vec));
+  return ADV_OK;
+}
+
+int adv_apply(adv_handle *h, const double *src, double *dst, double t, void *stream)
+{
+  if (!h || !src || !dst)
+    return fail(ADV_ERR_INVALID, "null argument");
+  if (int e = check_device(h))
+    return e;
+  cudaStream_t   s = (cudaStream_t)stream;
+  adv::StageArgs A = base_args(*h, t);
+  A.mode           = adv::kModeApply;
+  A.r_in           = src;
+  double *target   = dst;
+  if (src == dst)
+    {
+      if (int e = ensure_scratch(h, 0))
+        return e;
+      target = h->d_scratch[0];
+    }
+  A.r_out = target;
+  if (int e = launch(h, A, s))
+    return e;
+  if (target != dst)
+    ADV_CUDA(cudaMemcpyAsync(dst, target, h->mesh.n_dofs * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  return ADV_OK;
+}
+
+int adv_perform_stage(adv_handle *h, double t, double b_dt, double a_dt, const double *r_in,
+                      double *k, double *u, double *r_out, void *stream)
+{
+  if (!h || !r_in || !u || (a_dt != 0.0 && !r_out))
+    return fail(ADV_ERR_INVALID, "null argument");
+  if (a_dt != 0.0 && r_out == u)
+    return fail(ADV_ERR_ALIASING, "r_out must not alias u");
+  if (int e = check_device(h))
+    return e;
+  cudaStream_t   s   = (cudaStream_t)stream;
+  const size_t   nb  = h->mesh.n_dofs * sizeof(double);
+  adv::StageArgs A   = base_args(*h, t);
+  const double   fac = A.out_scale;
+  A.r_in             = r_in;
+  A.u_in             = u;
+  A.b                = b_dt * fac;
+  A.a                = a_dt * fac;
+  A.mode             = a_dt == 0.0 ? adv::kModeLastStage : adv::kModeStage;
+  // outputs must not alias r_in, which neighbouring cells read concurrently
+  double *u_target = u;
+  if (u == r_in)
+    {
+      if (k && k != r_in && k != r_out && k != u)
+        u_target = k;
+      else
+        {
+          if (int e = ensure_scratch(h, 0))
+            return e;
+          u_target = h->d_scratch[0];
+        }
+    }
+  double *r_target = r_out;
+  if (a_dt != 0.0 && r_out == r_in)
+    {
+      if (k && k != r_in && k != u && k != u_target)
+        r_target = k;
+      else
+        {
+          if (int e = ensure_scratch(h, 1))
+            return e;
+          r_target = h->d_scratch[1];
+        }
+    }
+  A.u_out = u_target;
+  A.r_out = a_dt != 0.0 ? r_target : nullptr;
+  if (int e = launch(h, A, s))
+    return e;
+  if (u_target != u)
+    ADV_CUDA(cudaMemcpyAsync(u, u_target, nb, cudaMemcpyDeviceToDevice, s));
+  if (a_dt != 0.0 && r_target != r_out)
+    ADV_CUDA(cudaMemcpyAsync(r_out, r_target, nb, cudaMemcpyDeviceToDevice, s));
+  return ADV_OK;
+}
+
+int adv_lsrk_coefficients(int scheme, double *a, double *b, int *n_stages)
+{
+  std::vector<double> av, bv;
+  if (!adv::lsrk_coefficients(scheme, av, bv))
+    return fail(ADV_ERR_INVALID, "unknown LSRK scheme");
+  if (a)
+    for (size_t i = 0; i < av.size(); ++i)
+      a[i] = av[i];
+  if (b)
+    for (size_t i = 0; i < bv.size(); ++i)
+      b[i] = bv[i];
+  if (n_stages)
+    *n_stages = (int)bv.size();
+  return ADV_OK;
+}
+
+// Time steps of LowStorageRungeKuttaIntegrator::perform_time_step
+// (advection_solver.cc:906-939) on caller buffers U (solution), R, K.
+// Stage 0 reads U and writes u' to K and r to R; stage 1 reads R, writes u'
+// back to U and r to K (each element of K is read as u before it is
+// overwritten as r by the same thread); later stages read r from the buffer
+// written by the previous stage, write the next r to the other one and
+// update U in place.  No stage writes a buffer that neighbouring cells read,
+// and the solution ends in U without copies.
+int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, double *u, double *r,
+                   double *k, void *stream)
+{
+  if (!h || !u || !r || !k)
+    return fail(ADV_ERR_INVALID, "null argument");
+  if (u == r || u == k || r == k)
+    return fail(ADV_ERR_ALIASING, "u, r and k must be distinct buffers");
+  if (n_steps < 0)
+    return fail(ADV_ERR_INVALID, "n_steps must be >= 0");
+  if (int e = check_device(h))
+    return e;
+  std::vector<double> ai, bi;
+  if (!adv::lsrk_coefficients(scheme, ai, bi))
+    return fail(ADV_ERR_INVALID, "unknown LSRK scheme");
+  cudaStream_t s  = (cudaStream_t)stream;
+  const int    ns = (int)bi.size();
+  for (int step = 0; step < n_steps; ++step)
+    {
+      const double t0 = t + step * dt;
+      double       sum_previous_bi = 0.0;
+      for (int st = 0; st < ns; ++st)
+        {
+          double ts = t0;
+          if (st > 0)
+            {
+              ts = t0 + (sum_previous_bi + ai[st - 1]) * dt;
+              sum_previous_bi += bi[st - 1];
+            }
+          adv::StageArgs A   = base_args(*h, ts);
+          const double   fac = A.out_scale;
+          const bool     last = st == ns - 1;
+          A.b                 = bi[st] * dt * fac;
+          A.a                 = last ? 0.0 : ai[st] * dt * fac;
+          A.mode              = last ? adv::kModeLastStage : adv::kModeStage;
+          if (st == 0)
+            {
+              A.r_in = u, A.u_in = u, A.u_out = k, A.r_out = r;
+            }
+          else if (st == 1)
+            {
+              A.r_in = r, A.u_in = k, A.u_out = u, A.r_out = k;
+            }
+          else
+            {
+              double *rin  = (st % 2 == 0) ? k : r;
+              double *rout = (st % 2 == 0) ? r : k;
+              A.r_in = rin, A.u_in = u, A.u_out = u, A.r_out = last ? nullptr : rout;
+            }
+          if (ns == 1)
+            {
+              // a one-stage scheme would leave the solution in K; not a scheme of the reference
+              return fail(ADV_ERR_INVALID, "one-stage schemes are not supported");
+            }
+          if (int e = launch(h, A, s))
+            return e;
+        }
+    }
+  return ADV_OK;
+}
+
+int adv_lsrk_step(adv_handle *h, int scheme, double t, double dt, double *u, double *r, double *k,
+                  void *stream)
+{
+  return adv_lsrk_steps(h, scheme, t, dt, 1, u, r, k, stream);
+}
+
+int adv_project(adv_handle *h, double t, double *dst, void *stream)
+{
+  if (!h || !dst)
+    return fail(ADV_ERR_INVALID, "null argument");
+  if (int e = check_device(h))
+    return e;
+  ADV_CUDA(adv::launch_project(h->diag, t, dst, (cudaStream_t)stream));
+  ++h->launches;
+  return ADV_OK;
+}
+
+int adv_mass_energy(adv_handle *h, const double *u, double out[3], void *stream)
+{
+  if (!h || !u || !out)
+    return fail(ADV_ERR_INVALID, "null argument");
+  if (int e = check_device(h))
+    return e;
+  cudaStream_t s = (cudaStream_t)stream;
+  int          nb = 0;
+  ADV_CUDA(adv::launch_mass_energy(h->diag, u, h->d_partials, &nb, s));
+  ++h->launches;
+  std::vector<double> part(3 * nb);
+  ADV_CUDA(cudaMemcpyAsync(part.data(), h->d_partials, part.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  ADV_CUDA(cudaStreamSynchronize(s));
+  out[0] = out[1] = out[2] = 0.0;
+  for (int b = 0; b < nb; ++b)
+    for (int i = 0; i < 3; ++i)
+      out[i] += part[3 * b + i];
+  return ADV_OK;
+}
+
+int adv_l2_error(adv_handle *h, const double *u, double t, double out[2], void *stream)
+{
+  if (!h || !u || !out)
+    return fail(ADV_ERR_INVALID, "null argument");
+  if (int e = check_device(h))
+    return e;
+  cudaStream_t s = (cudaStream_t)stream;
+  int          nb = 0;
+  ADV_CUDA(adv::launch_l2_error(h->diag, u, t, h->d_partials, &nb, s));
+  ++h->launches;
+  std::vector<double> part(3 * nb);
+  ADV_CUDA(cudaMemcpyAsync(part.data(), h->d_partials, part.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  ADV_CUDA(cudaStreamSynchronize(s));
+  double e2 = 0.0, n2 = 0.0;
+  for (int b = 0; b < nb; ++b)
+    e2 += part[3 * b], n2 += part[3 * b + 1];
+  out[0] = std::sqrt(e2);
+  out[1] = std::sqrt(n2);
+  return ADV_OK;
+}
+
+int adv_time_step(adv_handle *h, double courant, double *dt)
+{
+  if (!h || !dt)
+    return fail(ADV_ERR_INVALID, "null argument");
+  const double *a    = h->cfg.velocity;
+  const double  anrm = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+  if (!(anrm > 0.0))
+    return fail(ADV_ERR_INVALID, "zero velocity");
+  *dt = courant * h->h_min / anrm / std::pow(std::max(1, h->cfg.degree), 1.5);
+  return ADV_OK;
+}
+
+int adv_copy_to_host(adv_handle *h, const double *dev, double *host, void *stream)
+{
+  if (!h || !dev || !host)
+    return fail(ADV_ERR_INVALID, "null argument");
+  ADV_CUDA(cudaMemcpyAsync(host, dev, h->mesh.n_dofs * sizeof(double), cudaMemcpyDeviceToHost,
+                           (cudaStream_t)stream));
+  return ADV_OK;
+}
+
+int adv_copy_from_host(adv_handle *h, const double *host, double *dev, void *stream)
+{
+  if (!h || !dev || !host)
+    return fail(ADV_ERR_INVALID, "null argument");
+  ADV_CUDA(cudaMemcpyAsync(dev, host, h->mesh.n_dofs * sizeof(double), cudaMemcpyHostToDevice,
+                           (cudaStream_t)stream));
+  return ADV_OK;
+}
+
+int adv_measure_fma_peak(int precision, double *tflops, void *stream)
+{
+  if (!tflops || (precision != 0 && precision != 1))
+    return fail(ADV_ERR_INVALID, "bad argument");
+  cudaStream_t s   = (cudaStream_t)stream;
+  int          dev = 0, sms = 0;
+  ADV_CUDA(cudaGetDevice(&dev));
+  ADV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = sms * 8;
+  double   *buf    = nullptr;
+  ADV_CUDA(cudaMalloc(&buf, (size_t)blocks * 256 * sizeof(double)));
+  const int   iters = precision == 0 ? 4096 : 65536;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  int   rc   = ADV_OK;
+  for (int rep = 0; rep < 3 && rc == ADV_OK; ++rep)
+    {
+      cudaEventRecord(e0, s);
+      cudaError_t e = adv::launch_fma_peak(precision, buf, iters, blocks, s);
+      cudaEventRecord(e1, s);
+      if (e == cudaSuccess)
+        e = cudaEventSynchronize(e1);
+      if (e != cudaSuccess)
+        rc = cuda_fail(e, "fma peak kernel");
+      else
+        {
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          best = ms < best ? ms : best;
+        }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  if (rc)
+    return rc;
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * 256 / (best * 1e-3) / 1e12;
+  return ADV_OK;
+}
+
+} // extern "C"
+
+namespace adv
+{
+cudaError_t launch_stage(int n, int precision, const StageArgs &args, cudaStream_t stream)
+{
+  return precision == 0 ? launch_stage_fp64(n, args, stream) : launch_stage_fp32(n, args, stream);
+}
+int stage_cells_per_block(int n, int precision)
+{
+  return precision == 0 ? stage_cells_per_block_fp64(n) : stage_cells_per_block_fp32(n);
+}
+} // namespace adv

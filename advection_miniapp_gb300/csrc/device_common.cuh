@@ -1,0 +1,164 @@
+// Device-side helpers shared by the kernels: 1D tables in constant memory,
+// integer-pipe conversions between IEEE binary64 and binary32, and the
+// analytic solutions used for initial data, Dirichlet data and errors.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/advection_gb300.h"
+
+namespace adv
+{
+constexpr int kMaxNDev = 7;
+
+template <typename T>
+struct DevTables
+{
+  T S[kMaxNDev][kMaxNDev];  // nodal -> Gauss values
+  T Si[kMaxNDev][kMaxNDev]; // Gauss values -> nodal (S^{-1})
+  T Dw[kMaxNDev][kMaxNDev]; // weighted collocation derivative (integration by parts)
+  T D[kMaxNDev][kMaxNDev];  // collocation derivative on the Gauss points
+  T l0[kMaxNDev], l1[kMaxNDev];   // Gauss-Lagrange basis at xi = 0, 1
+  T lw0[kMaxNDev], lw1[kMaxNDev]; // the same divided by the Gauss weights
+  T gw[kMaxNDev];                 // Gauss weights
+};
+
+// Index [n] holds the tables of n points per direction.  The library is
+// built without relocatable device code, so every translation unit that
+// includes this header owns a copy, filled by its own upload function.
+static __constant__ DevTables<double> c_tab_d[kMaxNDev + 1];
+static __constant__ DevTables<float>  c_tab_f[kMaxNDev + 1];
+
+static inline cudaError_t upload_tables_local(const DevTables<double> *d, const DevTables<float> *f)
+{
+  cudaError_t e = cudaMemcpyToSymbol(c_tab_d, d, sizeof(c_tab_d));
+  if (e != cudaSuccess)
+    return e;
+  return cudaMemcpyToSymbol(c_tab_f, f, sizeof(c_tab_f));
+}
+
+template <typename T>
+__device__ __forceinline__ const DevTables<T> &tab(int n);
+template <>
+__device__ __forceinline__ const DevTables<double> &tab<double>(int n)
+{
+  return c_tab_d[n];
+}
+template <>
+__device__ __forceinline__ const DevTables<float> &tab<float>(int n)
+{
+  return c_tab_f[n];
+}
+
+// binary64 -> binary32 by integer arithmetic (round half away from zero in
+// magnitude; |x| below the smallest normal binary32 flushes to a signed
+// zero).  On this GPU F2F conversions issue on the FP64 pipe, which the
+// FP32-operator path otherwise reserves for the FP64 vector updates.
+__device__ __forceinline__ float d2f_int(double x)
+{
+  const long long b  = __double_as_longlong(x);
+  const unsigned  hi = (unsigned)((unsigned long long)b >> 32);
+  const unsigned  lo = (unsigned)b;
+  // exponent and top 23 mantissa bits, exponent rebased from 1023 to 127
+  const unsigned mag = __funnelshift_l(lo, hi, 3) + ((lo >> 28) & 1u) - 0xC0000000u;
+  const unsigned r   = ((hi & 0x7FF00000u) < 0x38100000u) ? 0u : mag;
+  return __uint_as_float(r | (hi & 0x80000000u));
+}
+
+// binary32 -> binary64, exact for normal numbers; subnormals become zero.
+__device__ __forceinline__ double f2d_int(float f)
+{
+  const unsigned b    = __float_as_uint(f);
+  const unsigned a    = b & 0x7FFFFFFFu;
+  const unsigned sign = b & 0x80000000u;
+  const bool     zero = a < 0x00800000u;
+  const unsigned hi   = zero ? sign : (sign | ((a >> 3) + 0x38000000u));
+  const unsigned lo   = zero ? 0u : (b << 29);
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+template <typename T>
+__device__ __forceinline__ T from_double(double x);
+template <>
+__device__ __forceinline__ double from_double<double>(double x)
+{
+  return x;
+}
+template <>
+__device__ __forceinline__ float from_double<float>(double x)
+{
+  return d2f_int(x);
+}
+
+template <typename T>
+__device__ __forceinline__ double to_double(T x);
+template <>
+__device__ __forceinline__ double to_double<double>(double x)
+{
+  return x;
+}
+template <>
+__device__ __forceinline__ double to_double<float>(float x)
+{
+  return f2d_int(x);
+}
+
+// Parameters of the analytic solution (initial data / Dirichlet data).
+struct ExactParams
+{
+  int    type;          // ADV_IC_*
+  int    constant_velocity;
+  double velocity[3];
+  double lo[3], L[3];
+  double p[8];
+};
+
+// The initial condition translated with the constant velocity (for the
+// rotating field: the initial condition).  Mirrors ExactSolution::value
+// (advection_solver.cc:149-172) for the workloads' initial data.
+__device__ __forceinline__ double exact_value(const ExactParams &e, double x0, double x1, double x2,
+                                              double t)
+{
+  const double kPi = 3.14159265358979323846;
+  const double tt  = e.constant_velocity ? t : 0.0;
+  const double x[3] = {x0, x1, x2};
+  if (e.type == ADV_IC_SINE_GAUSS)
+    {
+      double s[3], r2 = 0.0;
+      for (int d = 0; d < 3; ++d)
+        {
+          const double y = (x[d] - e.velocity[d] * tt - e.lo[d]) / e.L[d] - e.p[d];
+          s[d]           = y - floor(y);
+          r2 += (s[d] - 0.5) * (s[d] - 0.5);
+        }
+      return sin(2.0 * kPi * s[0]) * sin(2.0 * kPi * s[1]) * sin(2.0 * kPi * s[2]) + exp(-50.0 * r2);
+    }
+  if (e.type == ADV_IC_BLOB)
+    {
+      double r2 = 0.0;
+      for (int d = 0; d < 3; ++d)
+        {
+          const double y = x[d] - e.velocity[d] * tt - e.p[d];
+          r2 += y * y;
+        }
+      return exp(-r2 / (e.p[3] * e.p[3]));
+    }
+  double r = sin(4.0 * kPi * (x[0] - tt * e.velocity[0]));
+  r *= cos(4.0 * kPi * (x[1] - tt * e.velocity[1]));
+  r *= cos(4.0 * kPi * (x[2] - tt * e.velocity[2]));
+  return r;
+}
+
+// position of the deformed box (ADV_MESH_DEFORMED)
+__device__ __forceinline__ void deform_dev(double A, const double lo[3], const double L[3],
+                                           const double x[3], double y[3])
+{
+  const double kPi = 3.14159265358979323846;
+  double       s[3];
+  for (int d = 0; d < 3; ++d)
+    s[d] = (x[d] - lo[d]) / L[d];
+  for (int d = 0; d < 3; ++d)
+    y[d] = x[d] + A * L[d] * sin(2.0 * kPi * s[(d + 1) % 3]) * sin(2.0 * kPi * s[(d + 2) % 3]);
+}
+} // namespace adv

@@ -1,0 +1,92 @@
+// Host-visible launch interface of the CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "device_common.cuh"
+
+namespace adv
+{
+enum StageMode
+{
+  kModeApply     = 0, // r_out = out_scale * M^{-1} L r_in
+  kModeStage     = 1, // u_out = u_in + b k, r_out = u_in + a k
+  kModeLastStage = 2  // u_out = u_in + b k
+};
+
+// Arguments of the fused stage kernel (one launch = one LSRK stage or one
+// operator application).  r_in must not alias u_out or r_out; u_out may alias
+// u_in; r_out may alias u_in (each element is read before it is written by
+// the same thread).
+struct StageArgs
+{
+  const double *r_in;
+  const double *u_in;
+  double       *u_out;
+  double       *r_out;
+  double        b, a, out_scale;
+  int           mode;
+  int           swap_pm;  // velocity time factor < 0: exchange the upwind coefficients
+  int           nc[3];
+  int           npos[3];
+  long long     n_cells;
+  int           periodic;
+  int           uniform;  // affine mesh with constant velocity
+  int           bc_exact; // Dirichlet data from the exact solution (else zero)
+  int           pad0;
+  double        cv[3], P[3], M[3]; // uniform case: a_d / h_d and face coefficients
+  double        skew;
+  float         cvf[3], Pf[3], Mf[3], skewf; // the same in binary32 for the FP32 operator
+  int           has_skew;
+  int           pad1;
+  const void   *cell_geo;    // field case: [vt0|vt1|vt2|idet] x n^3 per cell (T)
+  const void   *face_geo[3]; // field case: [P|M] x n^2 per face (T)
+  const double *face_x[3];   // Dirichlet faces: n^2 x 3 coordinates per face
+  double        t;           // time of the Dirichlet data
+  ExactParams   ex;
+};
+
+// precision: 0 = FP64, 1 = FP32 operator
+cudaError_t launch_stage(int n, int precision, const StageArgs &args, cudaStream_t stream);
+// cells processed per CTA by the stage kernel (for launch accounting)
+int stage_cells_per_block(int n, int precision);
+
+// Upload the 1D tables (index n = points per direction) to every translation
+// unit's constant memory on the current device.
+cudaError_t upload_tables(const DevTables<double> *d, const DevTables<float> *f);
+cudaError_t upload_tables_stage64(const DevTables<double> *d, const DevTables<float> *f);
+cudaError_t upload_tables_stage32(const DevTables<double> *d, const DevTables<float> *f);
+cudaError_t upload_tables_diag(const DevTables<double> *d, const DevTables<float> *f);
+cudaError_t launch_stage_fp64(int n, const StageArgs &args, cudaStream_t stream);
+cudaError_t launch_stage_fp32(int n, const StageArgs &args, cudaStream_t stream);
+int stage_cells_per_block_fp64(int n);
+int stage_cells_per_block_fp32(int n);
+
+// Diagnostics and set-up kernels (diag_kernels.cu)
+struct DiagArgs
+{
+  int           n;
+  int           nc[3];
+  long long     n_cells;
+  double        lo[3], L[3], h[3];
+  int           curved;
+  int           pad0;
+  double        deformation;
+  ExactParams   ex;
+  // 1D data: Gauss-Lobatto nodes, Gauss points/weights (n), error-quadrature
+  // points/weights (n + 1); nodal basis values / derivatives at the Gauss
+  // points [q * n + i], S^{-1} [i * n + q]; at the error points [(n+1) x n]
+  double gl[8], gp[8], gw[8], ep[8], ew[8];
+  double S[49], Si[49], Sd[49];
+  double SE[56], SEd[56];
+};
+cudaError_t launch_project(const DiagArgs &g, double t, double *dst, cudaStream_t s);
+// partial sums per block written to `partials` (3 per block); returns number of blocks
+cudaError_t launch_mass_energy(const DiagArgs &g, const double *u, double *partials, int *n_blocks,
+                               cudaStream_t s);
+cudaError_t launch_l2_error(const DiagArgs &g, const double *u, double t, double *partials,
+                            int *n_blocks, cudaStream_t s);
+int diag_max_blocks(long long n_cells);
+cudaError_t launch_fma_peak(int precision, double *out, int iters, int blocks, cudaStream_t s);
+} // namespace adv

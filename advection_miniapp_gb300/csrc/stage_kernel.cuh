@@ -1,0 +1,455 @@
+// Fused matrix-free DG advection stage for sm_103a.
+//
+// One launch evaluates, for every cell, k = M^{-1} L(r_in) and applies the
+// low-storage Runge-Kutta update, replacing the reference's data.loop
+// (cell / inner-face / boundary-face workers, advection_solver.cc:469-631,
+// 710-718) followed by the inverse-mass cell_loop with its vector-update
+// lambda (advection_solver.cc:635-657, 722-752).
+//
+// Formulation (all in the space of the (k+1)^3 Gauss points of a cell):
+//   U   = (S x S x S) u                     values at the Gauss points
+//   Z   = idet * [ sum_d Dw_d (vt_d . U)    volume term, integrated by parts
+//                 + sum_faces lw(s) phi ]   face fluxes lifted to the points
+//   k   = (S^-1 x S^-1 x S^-1) Z            inverse mass matrix
+// Because the Gauss-Lobatto nodal basis and the Gauss points share the
+// tensor structure, S^-T cancels the transposed interpolation of the
+// integration step, so the exact cellwise inverse mass matrix of the
+// reference (CellwiseInverseMassMatrix, S^-1 diag(1/JxW) S^-T) costs one set
+// of three sweeps.  Face values of the own cell are contractions of the
+// Gauss-point values with l_q(0), l_q(1); neighbour values are its nodal face
+// layer (Gauss-Lobatto nodes include the end points) interpolated to the face
+// Gauss points.  Each face flux is computed from both sides, so no atomics
+// are needed and every cell is independent.
+//
+// Threads: one thread per 1D pencil of a cell, C cells per CTA; phases are
+// separated by __syncthreads.  The data of a CTA's cells stay in shared
+// memory from the load of r_in to the final sweep, whose output goes straight
+// from registers into the LSRK update.
+#pragma once
+
+#include "kernels.h"
+
+namespace adv
+{
+template <int N, typename T>
+struct StageShape
+{
+  static constexpr int cells()
+  {
+    if (sizeof(T) == 8)
+      return N == 2 ? 32 : N == 3 ? 32 : N == 4 ? 16 : N == 5 ? 16 : N == 6 ? 8 : 8;
+    return N == 2 ? 64 : N == 3 ? 32 : N == 4 ? 32 : N == 5 ? 32 : N == 6 ? 16 : 16;
+  }
+  static constexpr int C       = cells();
+  static constexpr int NQ      = N * N * N;
+  static constexpr int NF      = N * N;
+  static constexpr int WORK    = C * NF;
+  static constexpr int THREADS = ((WORK + 31) / 32) * 32;
+  static constexpr int SMEM    = (2 * NQ + 6 * NF) * C * (int)sizeof(T) + 2 * 6 * C * (int)sizeof(int);
+};
+
+// index of the point with coordinate a along direction d and (b, c) along
+// the sorted tangential directions of d
+template <int N>
+__device__ __forceinline__ int idx3(int d, int a, int b, int c)
+{
+  return d == 0 ? a + N * (b + N * c) : d == 1 ? b + N * (a + N * c) : b + N * (c + N * a);
+}
+
+// uniform-case constants in the operator's precision
+template <typename T>
+struct Consts;
+template <>
+struct Consts<double>
+{
+  static __device__ __forceinline__ double cv(const StageArgs &A, int d) { return A.cv[d]; }
+  static __device__ __forceinline__ double P(const StageArgs &A, int d) { return A.P[d]; }
+  static __device__ __forceinline__ double M(const StageArgs &A, int d) { return A.M[d]; }
+  static __device__ __forceinline__ double skew(const StageArgs &A) { return A.skew; }
+};
+template <>
+struct Consts<float>
+{
+  static __device__ __forceinline__ float cv(const StageArgs &A, int d) { return A.cvf[d]; }
+  static __device__ __forceinline__ float P(const StageArgs &A, int d) { return A.Pf[d]; }
+  static __device__ __forceinline__ float M(const StageArgs &A, int d) { return A.Mf[d]; }
+  static __device__ __forceinline__ float skew(const StageArgs &A) { return A.skewf; }
+};
+
+template <int N, typename T>
+__device__ __forceinline__ void sweep(const T (&M)[kMaxNDev][kMaxNDev], const T (&in)[N], T (&out)[N])
+{
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+    {
+      T s = M[q][0] * in[0];
+#pragma unroll
+      for (int i = 1; i < N; ++i)
+        s = fma(M[q][i], in[i], s);
+      out[q] = s;
+    }
+}
+
+// Face terms and volume term of one direction d for one pencil of Gauss-point
+// values U along d; returns the pencil's contribution to Z (without idet).
+template <int N, typename T, int D>
+__device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTables<T> &tb,
+                                               const T (&U)[N], T nlo, T nhi, int fq, int flo,
+                                               int fhi, const T *vt, int vstride, T (&out)[N])
+{
+  constexpr int NF = N * N;
+  T             ulo = tb.l0[0] * U[0], uhi = tb.l1[0] * U[0];
+#pragma unroll
+  for (int q = 1; q < N; ++q)
+    {
+      ulo = fma(tb.l0[q], U[q], ulo);
+      uhi = fma(tb.l1[q], U[q], uhi);
+    }
+  T Plo, Mlo, Phi, Mhi;
+  if (A.uniform)
+    {
+      Plo = Phi = Consts<T>::P(A, D);
+      Mlo = Mhi = Consts<T>::M(A, D);
+    }
+  else
+    {
+      const T *F = static_cast<const T *>(A.face_geo[D]);
+      Plo        = __ldg(F + (size_t)flo * 2 * NF + fq);
+      Mlo        = __ldg(F + (size_t)flo * 2 * NF + NF + fq);
+      Phi        = __ldg(F + (size_t)fhi * 2 * NF + fq);
+      Mhi        = __ldg(F + (size_t)fhi * 2 * NF + NF + fq);
+    }
+  if (A.swap_pm)
+    {
+      T tmp = Plo;
+      Plo   = Mlo, Mlo = tmp;
+      tmp   = Phi;
+      Phi   = Mhi, Mhi = tmp;
+    }
+  // numerical flux from the cell's point of view (outward normal):
+  //   low face (cell is the "plus" side):  phi = M u_own + P u_nbr
+  //   high face (cell is the "minus" side): phi = -P u_own - M u_nbr
+  // plus the skew-symmetric correction +-skew c u_own, c = P + M
+  T phlo = fma(Mlo, ulo, Plo * nlo);
+  T phhi = -fma(Phi, uhi, Mhi * nhi);
+  if (A.has_skew)
+    {
+      const T sk = Consts<T>::skew(A);
+      phlo       = fma(-sk * (Plo + Mlo), ulo, phlo);
+      phhi       = fma(sk * (Phi + Mhi), uhi, phhi);
+    }
+  T w[N];
+  if (A.uniform)
+    {
+#pragma unroll
+      for (int q = 0; q < N; ++q)
+        w[q] = U[q];
+    }
+  else
+    {
+#pragma unroll
+      for (int q = 0; q < N; ++q)
+        w[q] = __ldg(vt + q * vstride) * U[q];
+    }
+  sweep<N, T>(tb.Dw, w, out);
+  const T cv = Consts<T>::cv(A, D);
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+    {
+      T o = A.uniform ? cv * out[q] : out[q];
+      o   = fma(tb.lw0[q], phlo, o);
+      out[q] = fma(tb.lw1[q], phhi, o);
+    }
+}
+
+template <int N, typename T>
+__global__ void __launch_bounds__(StageShape<N, T>::THREADS)
+  stage_kernel(const StageArgs A)
+{
+  using SH                = StageShape<N, T>;
+  constexpr int C         = SH::C;
+  constexpr int NQ        = SH::NQ;
+  constexpr int NF        = SH::NF;
+  constexpr int NT        = SH::THREADS;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T   *Ub     = reinterpret_cast<T *>(smem_raw); // [C][NQ] nodal -> Gauss values
+  T   *Qb     = Ub + C * NQ;                     // [C][NQ] accumulated Z, then k
+  T   *Nb     = Qb + C * NQ;                     // [C][6][NF] neighbour face values
+  int *s_nbr  = reinterpret_cast<int *>(Nb + C * 6 * NF); // [C][6] neighbour cell or -1
+  int *s_face = s_nbr + C * 6;                            // [C][6] face id
+
+  const DevTables<T> &tb    = tab<T>(N);
+  const int           tid   = threadIdx.x;
+  const long long     cell0 = (long long)blockIdx.x * C;
+  const int           ncell = (int)min((long long)C, A.n_cells - cell0);
+
+  // ---- phase 0a: neighbour cells and face ids of the CTA's cells
+  for (int i = tid; i < ncell * 6; i += NT)
+    {
+      const int       cl = i / 6, j = i % 6, d = j >> 1, s = j & 1;
+      const long long c  = cell0 + cl;
+      const int       nx = A.nc[0], ny = A.nc[1], nz = A.nc[2];
+      const int       ix = (int)(c % nx), iy = (int)((c / nx) % ny), iz = (int)(c / ((long long)nx * ny));
+      // coordinate along d, its extent, and the sorted tangential coordinates
+      const int id  = d == 0 ? ix : d == 1 ? iy : iz;
+      const int nd  = d == 0 ? nx : d == 1 ? ny : nz;
+      const int j1  = d == 0 ? iy : ix;
+      const int j2  = d == 2 ? iy : iz;
+      const int n1  = d == 0 ? ny : nx;
+      const int npd = d == 0 ? A.npos[0] : d == 1 ? A.npos[1] : A.npos[2];
+      int       pos = id + s;
+      if (A.periodic && pos == nd)
+        pos = 0;
+      s_face[i] = pos + npd * (j1 + n1 * j2);
+      int nb    = id + (s ? 1 : -1);
+      if (A.periodic)
+        nb = (nb + nd) % nd;
+      if (nb < 0 || nb >= nd)
+        s_nbr[i] = -1;
+      else
+        {
+          const int jx = d == 0 ? nb : ix, jy = d == 1 ? nb : iy, jz = d == 2 ? nb : iz;
+          s_nbr[i] = (int)(jx + (long long)nx * (jy + (long long)ny * jz));
+        }
+    }
+  __syncthreads();
+
+  // ---- phase 0b: own values and the neighbours' nodal face layers
+  {
+    const double *src = A.r_in + cell0 * NQ;
+    for (int i = tid; i < ncell * NQ; i += NT)
+      Ub[i] = from_double<T>(__ldg(src + i));
+    for (int i = tid; i < ncell * 6 * NF; i += NT)
+      {
+        const int cf = i / NF, e = i % NF;
+        const int j = cf % 6, d = j >> 1, s = j & 1;
+        const int nb = s_nbr[cf];
+        T         v  = T(0);
+        if (nb >= 0)
+          v = from_double<T>(__ldg(A.r_in + (long long)nb * NQ + idx3<N>(d, s ? 0 : N - 1, e % N, e / N)));
+        Nb[i] = v;
+      }
+  }
+  __syncthreads();
+
+  // ---- phase 1: S along z; neighbour layers: S along the first tangential direction
+  for (int w = tid; w < ncell * NF; w += NT)
+    {
+      T  *p = Ub + (w / NF) * NQ + (w % NF);
+      T   in[N], out[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        in[k] = p[k * NF];
+      sweep<N, T>(tb.S, in, out);
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        p[k * NF] = out[k];
+    }
+  for (int w = tid; w < ncell * 6 * N; w += NT)
+    {
+      T *p = Nb + (w / N) * NF + (w % N) * N;
+      T  in[N], out[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        in[k] = p[k];
+      sweep<N, T>(tb.S, in, out);
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        p[k] = out[k];
+    }
+  __syncthreads();
+
+  // ---- phase 2: S along y; neighbour layers along the second tangential
+  //      direction, or Dirichlet data on boundary faces
+  for (int w = tid; w < ncell * NF; w += NT)
+    {
+      const int r = w % NF;
+      T        *p = Ub + (w / NF) * NQ + (r % N) + NF * (r / N);
+      T         in[N], out[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        in[k] = p[k * N];
+      sweep<N, T>(tb.S, in, out);
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        p[k * N] = out[k];
+    }
+  for (int w = tid; w < ncell * 6 * N; w += NT)
+    {
+      const int cf = w / N, q1 = w % N;
+      T        *p  = Nb + cf * NF + q1;
+      if (s_nbr[cf] >= 0)
+        {
+          T in[N], out[N];
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            in[k] = p[k * N];
+          sweep<N, T>(tb.S, in, out);
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            p[k * N] = out[k];
+        }
+      else
+        {
+          const int d = (cf % 6) >> 1;
+          for (int k = 0; k < N; ++k)
+            {
+              double g = 0.0;
+              if (A.bc_exact)
+                {
+                  const double *x = A.face_x[d] + ((size_t)s_face[cf] * NF + q1 + N * k) * 3;
+                  g               = exact_value(A.ex, x[0], x[1], x[2], A.t);
+                }
+              p[k * N] = from_double<T>(g);
+            }
+        }
+    }
+  __syncthreads();
+
+  // ---- phase 3: S along x gives the Gauss-point values; x-direction terms
+  for (int w = tid; w < ncell * NF; w += NT)
+    {
+      const int cl = w / NF, r = w % NF;
+      T        *p  = Ub + cl * NQ + N * r;
+      T         in[N], U[N], out[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        in[k] = p[k];
+      sweep<N, T>(tb.S, in, U);
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        p[k] = U[k];
+      const T *vt = A.uniform ? nullptr
+                              : static_cast<const T *>(A.cell_geo) + (cell0 + cl) * 4 * NQ + N * r;
+      direction_pass<N, T, 0>(A, tb, U, Nb[(cl * 6 + 0) * NF + r], Nb[(cl * 6 + 1) * NF + r], r,
+                              s_face[cl * 6 + 0], s_face[cl * 6 + 1], vt, 1, out);
+      T *z = Qb + cl * NQ + N * r;
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        z[k] = out[k];
+    }
+  __syncthreads();
+
+  // ---- phase 4: y-direction terms
+  for (int w = tid; w < ncell * NF; w += NT)
+    {
+      const int cl = w / NF, r = w % NF;
+      const int off = (r % N) + NF * (r / N);
+      const T  *p   = Ub + cl * NQ + off;
+      T         U[N], out[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        U[k] = p[k * N];
+      const T *vt = A.uniform ? nullptr
+                              : static_cast<const T *>(A.cell_geo) + ((cell0 + cl) * 4 + 1) * NQ + off;
+      direction_pass<N, T, 1>(A, tb, U, Nb[(cl * 6 + 2) * NF + r], Nb[(cl * 6 + 3) * NF + r], r,
+                              s_face[cl * 6 + 2], s_face[cl * 6 + 3], vt, N, out);
+      T *z = Qb + cl * NQ + off;
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        z[k * N] += out[k];
+    }
+  __syncthreads();
+
+  // ---- phase 5: z-direction terms, 1/det J, S^-1 along z
+  for (int w = tid; w < ncell * NF; w += NT)
+    {
+      const int cl = w / NF, r = w % NF;
+      const T  *p  = Ub + cl * NQ + r;
+      T         U[N], out[N], zz[N], kk[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        U[k] = p[k * NF];
+      const T *geo = A.uniform ? nullptr : static_cast<const T *>(A.cell_geo) + (cell0 + cl) * 4 * NQ;
+      direction_pass<N, T, 2>(A, tb, U, Nb[(cl * 6 + 4) * NF + r], Nb[(cl * 6 + 5) * NF + r], r,
+                              s_face[cl * 6 + 4], s_face[cl * 6 + 5], geo ? geo + 2 * NQ + r : nullptr,
+                              NF, out);
+      T *z = Qb + cl * NQ + r;
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        {
+          zz[k] = z[k * NF] + out[k];
+          if (!A.uniform)
+            zz[k] *= __ldg(geo + 3 * NQ + r + k * NF);
+        }
+      sweep<N, T>(tb.Si, zz, kk);
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        z[k * NF] = kk[k];
+    }
+  __syncthreads();
+
+  // ---- phase 6: S^-1 along y
+  for (int w = tid; w < ncell * NF; w += NT)
+    {
+      const int r = w % NF;
+      T        *p = Qb + (w / NF) * NQ + (r % N) + NF * (r / N);
+      T         in[N], out[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        in[k] = p[k * N];
+      sweep<N, T>(tb.Si, in, out);
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        p[k * N] = out[k];
+    }
+  __syncthreads();
+
+  // ---- phase 7: S^-1 along x, then the Runge-Kutta update from registers
+  for (int w = tid; w < ncell * NF; w += NT)
+    {
+      const int cl = w / NF, r = w % NF;
+      const T  *p  = Qb + cl * NQ + N * r;
+      T         in[N], kk[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        in[k] = p[k];
+      sweep<N, T>(tb.Si, in, kk);
+      const long long g = (cell0 + cl) * NQ + N * r;
+      if (A.mode == kModeApply)
+        {
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            A.r_out[g + k] = A.out_scale * to_double<T>(kk[k]);
+        }
+      else if (A.mode == kModeStage)
+        {
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            {
+              const double kd = to_double<T>(kk[k]);
+              const double u  = __ldcs(A.u_in + g + k);
+              A.u_out[g + k]  = fma(A.b, kd, u);
+              A.r_out[g + k]  = fma(A.a, kd, u);
+            }
+        }
+      else
+        {
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            {
+              const double kd = to_double<T>(kk[k]);
+              A.u_out[g + k]  = fma(A.b, kd, __ldcs(A.u_in + g + k));
+            }
+        }
+    }
+}
+
+template <int N, typename T>
+cudaError_t launch_stage_t(const StageArgs &args, cudaStream_t stream)
+{
+  using SH            = StageShape<N, T>;
+  static bool configured = false;
+  if (!configured)
+    {
+      cudaError_t e = cudaFuncSetAttribute(stage_kernel<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           SH::SMEM);
+      if (e != cudaSuccess)
+        return e;
+      configured = true;
+    }
+  const long long blocks = (args.n_cells + SH::C - 1) / SH::C;
+  stage_kernel<N, T><<<(unsigned)blocks, SH::THREADS, SH::SMEM, stream>>>(args);
+  return cudaGetLastError();
+}
+} // namespace adv

@@ -1,0 +1,392 @@
+"""Benchmark: GDoF/s per LSRK stage of the matrix-free DG advection operator.
+
+Workload (BASELINE configuration "plain method at GPU scale"): 64^3 cells of
+the sine-deformed unit cube (amplitude 0.08), FE_DGQ degree 4 (125 DoFs per
+cell, 32,768,000 DoFs), velocity (1, 0.15, -0.05), periodic, upwind flux,
+LSRK(5,4), Courant 0.5 / k^1.5, seeded analytic initial data.  One "step" is
+one LSRK(5,4) time step = 5 fused stage launches over the whole mesh.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm prints one JSON line: `value` is the FP64 operator's whole-job
+GDoF/s per stage with all data resident in HBM (three 262 MB vectors plus the
+geometry, larger than the 129 MB L2, so no flush is needed); `fp32_operator`
+holds the FP32-operator path (FP64 vectors) with its L2 error next to the FP64
+one; `e2e` repeats the FP64 measurement through the public Python API with a
+pinned-host -> device copy of the solution before and a device -> host copy
+after every step; `roofline` and `cpu_baseline` explain the numbers.  With
+--gpus N > 1 (torchrun) every rank solves its own replica (the path has no
+data exchange between independent solves): weak scaling.
+
+The reference arm (--impl reference) times the CPU oracle, the FP64 C++
+restatement of the reference's algorithm (the deal.II reference cannot be
+built here), with all host threads on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "deformed-k4-64"
+WORKLOAD_DESC = ("64^3 sine-deformed cells (amplitude 0.08), degree 4, 32,768,000 DoFs, "
+                 "velocity (1, 0.15, -0.05), periodic, upwind, LSRK(5,4), Courant 0.5/k^1.5")
+METRIC = "GDoF/s per LSRK stage, FP64 vs FP32-op at equal L2 error; p50/p99 solve latency"
+STAGES = 5
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# --------------------------------------------------------------------------
+# algorithmic work model of the fused stage kernel (per cell, n = k + 1)
+# --------------------------------------------------------------------------
+def fp_work_per_cell(n, curved=True):
+    """(FP instructions, flops with FMA = 2) of one fused stage per cell: three
+    interpolation sweeps, neighbour face interpolation (2 sweeps on 6 layers),
+    three direction passes (face traces, fluxes, volume derivative, lifts),
+    1/det J, three inverse-mass sweeps and the 2-FMA vector update."""
+    inst = 9 * n ** 4 + (30 if curved else 29) * n ** 3 + 12 * n ** 2
+    flops = 18 * n ** 4 + (47 if curved else 46) * n ** 3
+    return inst, flops
+
+
+def bytes_per_dof_step():
+    """FP64 vector bytes of one LSRK(5,4) step per DoF: stage 0 reads u and
+    writes u', r (24 B); stages 1-3 read r, u and write u, r (32 B); the last
+    stage reads r, u and writes u (24 B)."""
+    return 24 + 3 * 32 + 24
+
+
+def geometry_bytes_per_dof(n, word):
+    # per Gauss point 4 values (det J J^{-1} a, 1/det J); per face point 2 values, 3 faces per cell
+    return 4 * word + 3 * 2 * word / n
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# reference arm and CPU baseline: the oracle on the host cores
+# --------------------------------------------------------------------------
+def oracle_run(steps, warmup, time_budget=None):
+    from oracle import oracle as O
+    O.build()
+    threads = O.max_threads()
+    o = O.Oracle(degree=4, n_cells=(64, 64, 64), mesh_type=1, deformation=0.08)
+    dt = o.time_step(0.5)
+    u = o.project(0.0)
+    r, k = o.zeros(), o.zeros()
+    t = 0.0
+    for _ in range(warmup):
+        o.lsrk_step(t, dt, u, r, k)
+        t += dt
+    done = 0
+    t0 = time.perf_counter()
+    while done < steps:
+        o.lsrk_step(t, dt, u, r, k)
+        t += dt
+        done += 1
+        if time_budget is not None and time.perf_counter() - t0 > time_budget:
+            break
+    el = time.perf_counter() - t0
+    return dict(gdofs=o.n_dofs * STAGES * done / el / 1e9, seconds=el, steps=done, threads=threads,
+                n_dofs=o.n_dofs)
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    res = oracle_run(args.steps, args.warmup)
+    sample = (f"{res['steps']} full LSRK(5,4) steps of the {WORKLOAD} workload after {args.warmup} warm-up "
+              f"steps, {res['seconds']:.1f} s")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(res["gdofs"], 5), "unit": "GDoF/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": res["seconds"] / res["steps"] * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded analytic initial data)",
+        "config": {"workload": f"{WORKLOAD}: {WORKLOAD_DESC}", "arm": "CPU oracle (C++ FP64 restatement, OpenMP)"},
+        "cpu_baseline": {"value": round(res["gdofs"], 5), "unit": "GDoF/s", "cores": res["threads"],
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(res["gdofs"], 5), "unit": "GDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+# our arm
+# --------------------------------------------------------------------------
+def time_steps(torch, op, adv, u, r, k, dt, steps, warmup, stream):
+    with torch.cuda.stream(stream):
+        op.lsrk_steps(adv.LSRK_5_4, 0.0, dt, warmup, u, r, k, stream=stream)
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        op.lsrk_steps(adv.LSRK_5_4, warmup * dt, dt, steps, u, r, k, stream=stream)
+        e1.record(stream)
+        e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def run_precision(torch, adv, precision, args, stream, sampler_index):
+    op = adv.AdvectionOperation(adv.workload_config(WORKLOAD, precision=precision))
+    dt = op.time_step(0.5)
+    u = op.initialize_dof_vector()
+    op.project_initial(u)
+    r, k = op.initialize_dof_vector(), op.initialize_dof_vector()
+    torch.cuda.synchronize()
+    launches0 = op.launch_count()
+    with ClockSampler(sampler_index) as clk:
+        sec = time_steps(torch, op, adv, u, r, k, dt, args.steps, args.warmup, stream)
+    launches = op.launch_count() - launches0 - STAGES * args.warmup
+    err, nrm = op.l2_error(u, (args.warmup + args.steps) * dt)
+    return dict(op=op, u=u, r=r, k=k, dt=dt, seconds=sec, launches=launches, rel_l2=err / nrm,
+                clocks=clk.summary())
+
+
+def e2e_fp64(torch, adv, args, stream):
+    """FP64 through the public API with host copies of the solution around every step."""
+    op = adv.AdvectionOperation(adv.workload_config(WORKLOAD))
+    integ = adv.LowStorageRungeKuttaIntegrator(adv.LSRK_5_4)
+    dt = op.time_step(0.5)
+    u = op.initialize_dof_vector()
+    op.project_initial(u)
+    host = torch.empty(op.n_dofs, dtype=torch.float64, pin_memory=True)
+    host.copy_(u.cpu())
+    r, k = op.initialize_dof_vector(), op.initialize_dof_vector()
+    nb = op.n_dofs * 8
+
+    def step(t):
+        u.copy_(host, non_blocking=True)
+        integ.perform_time_step(op, t, dt, u, r, k, stream=stream)
+        host.copy_(u, non_blocking=True)
+
+    with torch.cuda.stream(stream):
+        for s in range(args.warmup):
+            step(s * dt)
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for s in range(args.steps):
+            step((args.warmup + s) * dt)
+        e1.record(stream)
+        e1.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    return dict(value=op.n_dofs * STAGES * args.steps / sec / 1e9, h2d=nb, d2h=nb)
+
+
+def ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import advection_miniapp_gb300 as adv
+    from advection_miniapp_gb300 import build as b
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    if rank == 0:
+        b.build()
+    if world > 1:
+        dist.barrier()
+    dev_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[local]) \
+        if os.environ.get("CUDA_VISIBLE_DEVICES") else local
+    stream = torch.cuda.Stream()
+
+    fp64_peak = adv.measure_fma_peak(adv.PRECISION_FP64, stream=stream)
+    fp32_peak = adv.measure_fma_peak(adv.PRECISION_FP32_OPERATOR, stream=stream)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    r64 = run_precision(torch, adv, adv.PRECISION_FP64, args, stream, dev_index)
+    n_dofs, n_cells = r64["op"].n_dofs, r64["op"].n_cells
+    del r64["op"], r64["u"], r64["r"], r64["k"]
+    torch.cuda.empty_cache()
+    barrier()
+    r32 = run_precision(torch, adv, adv.PRECISION_FP32_OPERATOR, args, stream, dev_index)
+    del r32["op"], r32["u"], r32["r"], r32["k"]
+    torch.cuda.empty_cache()
+    barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return t.item()
+
+    sec64, sec32 = max_over_ranks(r64["seconds"]), max_over_ranks(r32["seconds"])
+    units = n_dofs * STAGES * args.steps * world
+    v64, v32 = units / sec64 / 1e9, units / sec32 / 1e9
+
+    e2e = None
+    if not args.no_e2e:
+        e = e2e_fp64(torch, adv, args, stream)
+        e2e = {"value": round(e["value"] * world, 4), "unit": "GDoF/s", "h2d_bytes_per_step": e["h2d"],
+               "d2h_bytes_per_step": e["d2h"]}
+    barrier()
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    n = 5
+    launch64 = r64["seconds"] / (STAGES * args.steps)
+    launch32 = r32["seconds"] / (STAGES * args.steps)
+    inst, flops = fp_work_per_cell(n)
+    vec_bytes_launch = bytes_per_dof_step() / STAGES * n_dofs
+    achieved64 = flops * n_cells / launch64 / 1e12
+    achieved32_hbm = vec_bytes_launch / launch32 / 1e9
+    geo32 = geometry_bytes_per_dof(n, 4) * n_dofs / launch32 / 1e9
+    geo64 = geometry_bytes_per_dof(n, 8) * n_dofs / launch64 / 1e9
+    hbm_peak = 6780.7
+    peaks_file = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_file):
+        hbm_peak = json.load(open(peaks_file)).get("hbm_gbs", hbm_peak)
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        res = oracle_run(steps=10, warmup=0, time_budget=20.0)
+        cpu = {"value": round(res["gdofs"], 5), "unit": "GDoF/s", "cores": res["threads"], "kind": "port",
+               "sample": f"{res['steps']} LSRK(5,4) steps of the full {WORKLOAD} workload on the host cores "
+                         f"({res['seconds']:.1f} s) by the FP64 C++ oracle"}
+
+    line = {
+        "metric": METRIC,
+        "value": round(v64, 4),
+        "unit": "GDoF/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(sec64 / args.steps * 1e3, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded analytic initial data on the deformed mesh; no dataset)",
+        "config": {"workload": f"{WORKLOAD}: {WORKLOAD_DESC}", "precision": "FP64 operator, FP64 vectors",
+                   "l2": "inputs larger than L2 (three 262 MB FP64 vectors + geometry per stage)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "rel_l2_error": r64["rel_l2"],
+        "roofline": {"bound": "fp64", "achieved": round(achieved64, 4), "peak": round(fp64_peak, 4),
+                     "unit": "TFLOP/s", "frac": round(achieved64 / fp64_peak, 4), "traffic": None,
+                     "peak_source": "FP64 FMA microbenchmark (adv_measure_fma_peak) on this GPU",
+                     "flops_per_cell": flops, "fp64_inst_per_cell": inst,
+                     "hbm_achieved_gbs": round(vec_bytes_launch / launch64 / 1e9 + geo64, 2),
+                     "hbm_frac_of_measured": round((vec_bytes_launch / launch64 / 1e9 + geo64) / hbm_peak, 4),
+                     "launch_ms": round(launch64 * 1e3, 4)},
+        "fp32_operator": {
+            "value": round(v32, 4), "unit": "GDoF/s", "speedup_vs_fp64": round(v32 / v64, 3),
+            "rel_l2_error": r32["rel_l2"], "fp64_rel_l2_error": r64["rel_l2"],
+            "l2_error_ratio": round(r32["rel_l2"] / r64["rel_l2"], 6),
+            "ms_per_step": round(sec32 / args.steps * 1e3, 4),
+            "roofline": {"bound": "hbm", "achieved": round(achieved32_hbm, 2), "peak": hbm_peak, "unit": "GB/s",
+                         "frac": round(achieved32_hbm / hbm_peak, 4), "traffic": None,
+                         "geometry_gbs": round(geo32, 2),
+                         "frac_with_geometry": round((achieved32_hbm + geo32) / hbm_peak, 4),
+                         "fp32_flops_tflops": round(flops * n_cells / launch32 / 1e12, 3),
+                         "fp32_peak_tflops": round(fp32_peak, 3), "launch_ms": round(launch32 * 1e3, 4)},
+            "clocks": r32["clocks"]},
+        "e2e": e2e,
+        "gpu_launches": r64["launches"] + r32["launches"],
+        "clocks": r64["clocks"],
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        ours(args)
+
+
+if __name__ == "__main__":
+    main()

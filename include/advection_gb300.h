@@ -1,0 +1,162 @@
+/*
+ * advection_gb300: C ABI of the GB300-native (sm_103a) matrix-free DG
+ * advection operator and its low-storage Runge-Kutta stage.
+ *
+ * The reference (kronbichler/advection_miniapp) exposes this path as a C++
+ * class used through templates, not as an FFI.  Each entry point below names
+ * the reference member it replaces; a C++ wrapper with the reference's own
+ * call surface (AdvectionOperation / LowStorageRungeKuttaIntegrator) sits on
+ * top in advection_gb300.hpp.
+ *
+ * Conventions
+ *  - Vectors are caller-owned device buffers of n_dofs values (double unless
+ *    stated), laid out cell by cell (cells lexicographic, x fastest) and,
+ *    inside a cell, lexicographic over the (k+1)^3 Gauss-Lobatto support
+ *    points (x fastest), like FE_DGQ's numbering.  adv_alloc_vector is a
+ *    convenience; any cudaMalloc'ed buffer of the right size works.
+ *  - Every call takes an explicit CUDA stream (NULL = legacy default stream)
+ *    and returns an int status: 0 = ok, see ADV_ERR_*.  No exception crosses
+ *    the ABI.  adv_last_error() gives a message for the calling thread.
+ *  - A handle is not thread-safe (the reference operator is not re-entrant
+ *    either: its `time` member is written in const methods,
+ *    advection_solver.cc:397,706); distinct handles are independent.
+ */
+#ifndef ADVECTION_GB300_H
+#define ADVECTION_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum
+{
+  ADV_OK               = 0,
+  ADV_ERR_INVALID      = 1, /* bad argument or unsupported configuration */
+  ADV_ERR_OUT_OF_MEMORY = 2,
+  ADV_ERR_CUDA         = 3, /* a CUDA runtime call failed */
+  ADV_ERR_ALIASING     = 4, /* vector aliasing pattern that cannot be honoured */
+  ADV_ERR_NOT_CONVERGED = 5,
+  ADV_ERR_TIMEOUT      = 6
+};
+
+/* ----------------------------------------------------------- enumerations */
+enum { ADV_MESH_CARTESIAN = 0, ADV_MESH_DEFORMED = 1 };
+enum { ADV_VELOCITY_CONSTANT = 0, ADV_VELOCITY_ROTATING = 1 };
+enum { ADV_IC_SINE_GAUSS = 0, ADV_IC_BLOB = 1, ADV_IC_WAVE = 2 };
+enum { ADV_BOUNDARY_ZERO = 0, ADV_BOUNDARY_EXACT = 1 };
+enum { ADV_PRECISION_FP64 = 0, ADV_PRECISION_FP32_OPERATOR = 1 };
+/* LSRK schemes in the order of the reference's enum (advection_solver.cc:83-89) */
+enum { ADV_LSRK_3_3 = 0, ADV_LSRK_5_4 = 1, ADV_LSRK_7_4 = 2, ADV_LSRK_9_5 = 3 };
+
+/*
+ * Run-time replacement of the reference's compile-time parameter block
+ * (advection_solver.cc:55-123; degree was a template argument there).
+ */
+typedef struct adv_config
+{
+  int32_t degree;            /* FE_DGQ degree k, 1..6 (n = k+1 points per direction) */
+  int32_t n_cells[3];        /* structured hex mesh, cells per direction */
+  double  domain_lo[3];      /* box corners (unit cube in the workloads) */
+  double  domain_hi[3];
+  int32_t mesh_type;         /* ADV_MESH_*: affine, or sine-deformed with a degree-k mapping */
+  int32_t periodic;          /* 1: periodic in every direction; 0: Dirichlet on every face */
+  double  deformation;       /* A in x_d += A L_d sin(2 pi s_{d+1}) sin(2 pi s_{d+2}) */
+  int32_t velocity_type;     /* ADV_VELOCITY_* */
+  int32_t initial_condition; /* ADV_IC_*: initial data / exact solution */
+  double  velocity[3];       /* constant velocity, or amplitudes of the rotating field */
+  double  velocity_period;   /* T in cos(pi t / T) of the rotating field */
+  double  flux_alpha;        /* 1: upwind (Lax-Friedrichs), 0: central (advection_solver.cc:74-75) */
+  double  factor_skew;       /* 0: conservative, 0.5: skew-symmetric (advection_solver.cc:106-108) */
+  double  diffusion;         /* SIPG diffusivity; 0 disables the viscous terms */
+  double  penalty_factor;    /* SIPG penalty sigma = penalty_factor (k+1)^2 / h */
+  int32_t boundary_value;    /* ADV_BOUNDARY_*: Dirichlet data zero or the exact solution */
+  int32_t reserved0;
+  double  ic_params[8];      /* sine-Gauss: phase p[3]; blob: centre c[3], width w */
+  /* ---- fields below have no counterpart in the oracle's configuration ---- */
+  int32_t precision;         /* ADV_PRECISION_*: FP64, or FP32 operator with FP64 vectors */
+  int32_t reserved1[7];
+} adv_config;
+
+typedef struct adv_handle adv_handle;
+
+/* Fills *cfg with the defaults of the constant-velocity periodic workload
+ * (degree 3, 8^3 cells, velocity (1, 0.15, -0.05), upwind flux, FP64). */
+void adv_config_default(adv_config *cfg);
+
+/* AdvectionOperation::reinit (advection_solver.cc:435-465): builds the mesh,
+ * the 1D tables and the geometry on the current device and uploads them. */
+int adv_create(const adv_config *cfg, adv_handle **out);
+/* AdvectionOperation destructor (advection_solver.cc:349-372): frees device data. */
+int adv_destroy(adv_handle *h);
+const char *adv_last_error(void);
+
+int adv_n_dofs(const adv_handle *h, int64_t *out);
+int adv_n_cells(const adv_handle *h, int64_t *out);
+/* Device bytes held by the handle (geometry, tables, scratch). */
+int adv_device_bytes(const adv_handle *h, int64_t *out);
+
+/* AdvectionOperation::initialize_dof_vector (advection_solver.cc:343-347). */
+int adv_alloc_vector(adv_handle *h, double **out);
+int adv_free_vector(adv_handle *h, double *vec);
+
+/* AdvectionOperation::apply (advection_solver.cc:661-691): dst = M^{-1} L(t) src.
+ * dst may alias src. */
+int adv_apply(adv_handle *h, const double *src, double *dst, double t, void *stream);
+
+/* AdvectionOperation::perform_stage (advection_solver.cc:695-756):
+ *   k = M^{-1} L(t) r_in;  u <- u + b_dt k;  r_out <- u_old + a_dt k (a_dt != 0).
+ * Honours the reference's aliasing patterns (r_in == u with k == r_out on the
+ * first stage, r_in == r_out on later stages).  `k` is scratch: its contents
+ * afterwards are unspecified. */
+int adv_perform_stage(adv_handle *h, double t, double b_dt, double a_dt, const double *r_in,
+                      double *k, double *u, double *r_out, void *stream);
+
+/* LowStorageRungeKuttaIntegrator::perform_time_step (advection_solver.cc:906-939):
+ * one step of scheme ADV_LSRK_* from time t with step dt.  u holds the solution;
+ * r and k are scratch registers (unspecified contents afterwards). */
+int adv_lsrk_step(adv_handle *h, int scheme, double t, double dt, double *u, double *r, double *k,
+                  void *stream);
+/* n_steps consecutive steps (the reference's time loop, advection_solver.cc:1275-1300,
+ * without output). */
+int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, double *u,
+                   double *r, double *k, void *stream);
+/* Number of stages and the (a, b) coefficients of a scheme (a has n_stages-1 entries). */
+int adv_lsrk_coefficients(int scheme, double *a, double *b, int *n_stages);
+
+/* AdvectionOperation::project_initial (advection_solver.cc:760-784) of the
+ * exact solution at time t (t = 0: the initial condition). */
+int adv_project(adv_handle *h, double t, double *dst, void *stream);
+
+/* compute_mass_and_energy (advection_solver.cc:787-818): out = {int u, int u^2,
+ * int |grad u|^2}.  Synchronises the stream. */
+int adv_mass_energy(adv_handle *h, const double *u, double out[3], void *stream);
+
+/* output_results' error (advection_solver.cc:1183-1208): out[0] = ||u - u_exact(t)||
+ * with QGauss(k+2), out[1] = ||u_exact(t)|| with QGauss(k+1).  Synchronises. */
+int adv_l2_error(adv_handle *h, const double *u, double t, double out[2], void *stream);
+
+/* setup_dofs time step rule (advection_solver.cc:1155-1165), before rounding:
+ * courant * h_min / |a| / k^1.5. */
+int adv_time_step(adv_handle *h, double courant, double *dt);
+
+/* Host <-> device copies of whole vectors (stream-ordered; synchronise before
+ * reading host data). */
+int adv_copy_to_host(adv_handle *h, const double *dev, double *host, void *stream);
+int adv_copy_from_host(adv_handle *h, const double *host, double *dev, void *stream);
+
+/* Number of kernel launches the library has issued on this handle. */
+int adv_launch_count(const adv_handle *h, int64_t *out);
+
+/* Measured FP64 / FP32 fused multiply-add throughput of the current device in
+ * TFLOP/s (FMA = 2 flops), for roofline denominators.  Synchronises. */
+int adv_measure_fma_peak(int precision, double *tflops, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

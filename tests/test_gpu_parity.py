@@ -1,0 +1,250 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Bars: FP64 operator results within 1e-12 relative (max norm, scaled by the
+largest reference entry) of the oracle; the FP32-operator path within 5e-6 of
+it (FP32 arithmetic on O(1) data with FP64 vectors).
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+FP64_TOL = 1e-12
+FP32_TOL = 5e-6
+
+CASES = {
+    "affine-k1": dict(degree=1, n_cells=(3, 2, 4)),
+    "affine-k2": dict(degree=2, n_cells=(3, 3, 3)),
+    "affine-k3": dict(degree=3, n_cells=(4, 3, 5)),
+    "affine-k4": dict(degree=4, n_cells=(3, 3, 3)),
+    "affine-k5": dict(degree=5, n_cells=(2, 3, 2)),
+    "affine-k6": dict(degree=6, n_cells=(2, 2, 3)),
+    "single-cell-periodic": dict(degree=3, n_cells=(1, 1, 1)),
+    "curved-k4": dict(degree=4, n_cells=(4, 4, 4), mesh_type=1, deformation=0.08),
+    "curved-k2-dirichlet": dict(degree=2, n_cells=(3, 2, 2), mesh_type=1, deformation=0.06, periodic=0,
+                                initial_condition=2),
+    "affine-k3-dirichlet-skew": dict(degree=3, n_cells=(2, 3, 2), periodic=0, factor_skew=0.5,
+                                     initial_condition=2),
+    "affine-k2-central": dict(degree=2, n_cells=(3, 3, 3), flux_alpha=0.0),
+    "rotating-k3": dict(degree=3, n_cells=(3, 3, 2), periodic=0, velocity_type=1, velocity=(1.0, 1.0, 0.3),
+                        velocity_period=0.5, initial_condition=1, ic_params=(0.3, 0.5, 0.5, 0.1),
+                        boundary_value=0),
+    "box-domain": dict(degree=3, n_cells=(2, 3, 4), domain_lo=(-1.0, 0.0, 0.5), domain_hi=(1.0, 0.5, 2.0),
+                       velocity=(0.3, -0.7, 0.2)),
+}
+
+
+def pair(oracle_mod, adv, cfg, precision=0):
+    o = oracle_mod.Oracle(**cfg)
+    g = adv.AdvectionOperation(**cfg, precision=precision)
+    assert g.n_dofs == o.n_dofs
+    return o, g
+
+
+def to_dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def rel_err(a, ref):
+    return np.abs(np.asarray(a) - ref).max() / max(np.abs(ref).max(), 1e-300)
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+@pytest.mark.parametrize("precision", [0, 1])
+def test_apply_matches_oracle(cuda, oracle_mod, adv_lib, case, precision):
+    torch = cuda
+    o, g = pair(oracle_mod, adv_lib, CASES[case], precision)
+    rng = np.random.default_rng(7)
+    src = rng.standard_normal(o.n_dofs)
+    for t in (0.0, 0.31, 0.4):  # the rotating field's factor cos(pi t / 0.5) changes sign at 0.25
+        ref = o.apply(src, t)
+        s = to_dev(torch, src)
+        d = g.initialize_dof_vector()
+        g.apply(s, d, t)
+        torch.cuda.synchronize()
+        err = rel_err(d.cpu().numpy(), ref)
+        assert err <= (FP64_TOL if precision == 0 else FP32_TOL), (case, t, err)
+        # in-place application (dst == src)
+        g.apply(s, s, t)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(s.cpu().numpy(), d.cpu().numpy())
+
+
+@pytest.mark.parametrize("case", ["affine-k3", "curved-k4", "rotating-k3", "affine-k3-dirichlet-skew"])
+def test_perform_stage_aliasing_patterns(cuda, oracle_mod, adv_lib, case):
+    torch = cuda
+    o, g = pair(oracle_mod, adv_lib, CASES[case])
+    rng = np.random.default_rng(11)
+    u0, r0 = rng.standard_normal(o.n_dofs), rng.standard_normal(o.n_dofs)
+    b, a, t = 0.013, 0.021, 0.3
+    # stage 0 of the reference integrator: perform_stage(t, b, a, u, r, u, r)
+    uo, ro = u0.copy(), np.zeros_like(u0)
+    o.perform_stage(t, b, a, uo, ro, uo, ro)
+    u, r = to_dev(torch, u0), g.initialize_dof_vector()
+    g.perform_stage(t, b, a, u, r, u, r)
+    torch.cuda.synchronize()
+    assert rel_err(u.cpu().numpy(), uo) <= FP64_TOL
+    assert rel_err(r.cpu().numpy(), ro) <= FP64_TOL
+    # later stage: perform_stage(t, b, a, r, k, u, r)
+    uo, ro, ko = u0.copy(), r0.copy(), np.zeros_like(u0)
+    o.perform_stage(t, b, a, ro, ko, uo, ro)
+    u, r, k = to_dev(torch, u0), to_dev(torch, r0), g.initialize_dof_vector()
+    g.perform_stage(t, b, a, r, k, u, r)
+    torch.cuda.synchronize()
+    assert rel_err(u.cpu().numpy(), uo) <= FP64_TOL
+    assert rel_err(r.cpu().numpy(), ro) <= FP64_TOL
+    # last stage (a == 0): only u is updated
+    uo, ro = u0.copy(), r0.copy()
+    o.perform_stage(t, b, 0.0, ro, ko, uo, ro)
+    u, r = to_dev(torch, u0), to_dev(torch, r0)
+    g.perform_stage(t, b, 0.0, r, k, u, r)
+    torch.cuda.synchronize()
+    assert rel_err(u.cpu().numpy(), uo) <= FP64_TOL
+    # no aliasing at all
+    uo, ro = u0.copy(), np.zeros_like(u0)
+    rin = rng.standard_normal(o.n_dofs)
+    o.perform_stage(t, b, a, rin, ko, uo, ro)
+    u, r = to_dev(torch, u0), g.initialize_dof_vector()
+    g.perform_stage(t, b, a, to_dev(torch, rin), g.initialize_dof_vector(), u, r)
+    torch.cuda.synchronize()
+    assert rel_err(u.cpu().numpy(), uo) <= FP64_TOL
+    assert rel_err(r.cpu().numpy(), ro) <= FP64_TOL
+
+
+@pytest.mark.parametrize("scheme", [0, 1, 2, 3])
+@pytest.mark.parametrize("case", ["affine-k3", "curved-k4", "rotating-k3"])
+def test_lsrk_steps_match_oracle(cuda, oracle_mod, adv_lib, case, scheme):
+    torch = cuda
+    o, g = pair(oracle_mod, adv_lib, CASES[case])
+    dt = o.time_step(0.5)
+    u = o.project(0.0)
+    r, k = o.zeros(), o.zeros()
+    ud = to_dev(torch, u)
+    rd, kd = g.initialize_dof_vector(), g.initialize_dof_vector()
+    t0 = 0.17
+    for s in range(3):
+        o.lsrk_step(t0 + s * dt, dt, u, r, k, scheme)
+    g.lsrk_steps(scheme, t0, dt, 3, ud, rd, kd)
+    torch.cuda.synchronize()
+    assert rel_err(ud.cpu().numpy(), u) <= FP64_TOL
+
+
+def test_integrator_stage_loop_equals_fused_step(cuda, adv_lib):
+    """The reference's stage loop through perform_stage and the fused step agree."""
+    torch = cuda
+    g = adv_lib.AdvectionOperation(**CASES["curved-k4"])
+    integ = adv_lib.LowStorageRungeKuttaIntegrator(adv_lib.LSRK_5_4)
+
+    class StageOnly:  # forces the generic stage loop of perform_time_step
+        def __init__(self, op):
+            self.op = op
+
+        def perform_stage(self, *args):
+            self.op.perform_stage(*args)
+
+    dt = g.time_step(0.5)
+    u1 = g.initialize_dof_vector()
+    g.project_initial(u1)
+    u2 = u1.clone()
+    r1, k1, r2, k2 = (g.initialize_dof_vector() for _ in range(4))
+    for s in range(4):
+        integ.perform_time_step(g, s * dt, dt, u1, r1, k1)
+        integ.perform_time_step(StageOnly(g), s * dt, dt, u2, r2, k2)
+    torch.cuda.synchronize()
+    assert rel_err(u1.cpu().numpy(), u2.cpu().numpy()) <= 1e-14
+
+
+@pytest.mark.parametrize("case", ["affine-k3", "curved-k4", "rotating-k3", "affine-k6"])
+def test_projection_mass_energy_l2(cuda, oracle_mod, adv_lib, case):
+    torch = cuda
+    o, g = pair(oracle_mod, adv_lib, CASES[case])
+    u = o.project(0.0)
+    ud = g.initialize_dof_vector()
+    g.project_initial(ud)
+    torch.cuda.synchronize()
+    assert rel_err(ud.cpu().numpy(), u) <= 1e-13
+    me_o = o.mass_energy(u)
+    me_g = g.compute_mass_and_energy(ud)
+    np.testing.assert_allclose(me_g, me_o, rtol=1e-12, atol=1e-14)
+    rng = np.random.default_rng(5)
+    w = u + 1e-3 * rng.standard_normal(o.n_dofs)
+    eo, no = o.l2_error(w, 0.2)
+    eg, ng = g.l2_error(to_dev(torch, w), 0.2)
+    assert abs(eg - eo) <= 1e-12 * eo and abs(ng - no) <= 1e-12 * no
+
+
+def test_config1_against_golden(cuda, adv_lib):
+    """8^3 affine, degree 3, 200 LSRK(5,4) steps: final vector and L2 error."""
+    torch = cuda
+    gold = np.load(os.path.join(GOLDEN, "cartesian_k3_8.npz"))
+    g = adv_lib.AdvectionOperation(adv_lib.workload_config("cartesian-k3-8"))
+    dt = g.time_step(0.5)
+    assert abs(dt - float(gold["dt"])) < 1e-16
+    u = g.initialize_dof_vector()
+    g.project_initial(u)
+    r, k = g.initialize_dof_vector(), g.initialize_dof_vector()
+    g.lsrk_steps(adv_lib.LSRK_5_4, 0.0, dt, 200, u, r, k)
+    err, nrm = g.l2_error(u, float(gold["t_end"]))
+    final = u.cpu().numpy()
+    assert rel_err(final, gold["u_final"]) <= 1e-11
+    assert abs(err / nrm - float(gold["rel_l2"])) <= 1e-9 * float(gold["rel_l2"])
+    me = g.compute_mass_and_energy(u)
+    np.testing.assert_allclose(me, gold["mass_energy"], rtol=1e-11, atol=1e-14)
+
+
+def test_operator_golden_fixtures(cuda, adv_lib):
+    import sys
+    torch = cuda
+    sys.path.insert(0, GOLDEN)
+    from gen_golden import OPERATOR_CASES
+    gold = np.load(os.path.join(GOLDEN, "operator_cases.npz"))
+    for name, cfg in OPERATOR_CASES.items():
+        g = adv_lib.AdvectionOperation(**cfg)
+        d = g.initialize_dof_vector()
+        g.apply(to_dev(torch, gold[name + "_src"]), d, 0.25)
+        torch.cuda.synchronize()
+        assert rel_err(d.cpu().numpy(), gold[name + "_dst"]) <= FP64_TOL, name
+
+
+def test_fp32_operator_l2_error_matches_fp64(cuda, adv_lib):
+    """FP32 operator with FP64 vectors: same L2 error as FP64 within 1.05x (16^3 curved, k=4)."""
+    torch = cuda
+    errs = []
+    for precision in (0, 1):
+        g = adv_lib.AdvectionOperation(adv_lib.workload_config("deformed-k4-64", precision=precision,
+                                                               n_cells=(16, 16, 16)))
+        dt = g.time_step(0.5)
+        u = g.initialize_dof_vector()
+        g.project_initial(u)
+        r, k = g.initialize_dof_vector(), g.initialize_dof_vector()
+        g.lsrk_steps(adv_lib.LSRK_5_4, 0.0, dt, 40, u, r, k)
+        e, n = g.l2_error(u, 40 * dt)
+        errs.append(e / n)
+    assert errs[1] <= 1.05 * errs[0], errs
+
+
+def test_full_size_curved_properties(cuda, adv_lib):
+    """64^3 curved, degree 4 (32.8M DoFs): mass conserved, energy non-increasing,
+    FP32-operator result close to FP64 after a few steps."""
+    torch = cuda
+    res = {}
+    for precision in (0, 1):
+        g = adv_lib.AdvectionOperation(adv_lib.workload_config("deformed-k4-64", precision=precision))
+        dt = g.time_step(0.5)
+        u = g.initialize_dof_vector()
+        g.project_initial(u)
+        m0 = g.compute_mass_and_energy(u)
+        r, k = g.initialize_dof_vector(), g.initialize_dof_vector()
+        g.lsrk_steps(adv_lib.LSRK_5_4, 0.0, dt, 3, u, r, k)
+        m1 = g.compute_mass_and_energy(u)
+        # each face flux is evaluated from both sides: conservation holds to round-off
+        tol = 1e-12 if precision == 0 else 1e-6
+        assert abs(m1[0] - m0[0]) <= tol * max(1.0, abs(m0[1])), precision
+        assert m1[1] <= m0[1] * (1 + 1e-12)
+        res[precision] = u.cpu().numpy()
+        del g, u, r, k
+        torch.cuda.empty_cache()
+    assert rel_err(res[1], res[0]) <= 1e-5
