@@ -438,15 +438,20 @@ __global__ void __launch_bounds__(StageShape<N, T>::THREADS)
 template <int N, typename T>
 cudaError_t launch_stage_t(const StageArgs &args, cudaStream_t stream)
 {
-  using SH            = StageShape<N, T>;
-  static bool configured = false;
-  if (!configured)
+  using SH = StageShape<N, T>;
+  // the shared-memory opt-in is a per-device function attribute
+  static unsigned long long configured = 0;
+  int                       dev        = 0;
+  cudaError_t               e          = cudaGetDevice(&dev);
+  if (e != cudaSuccess)
+    return e;
+  if (dev >= 64 || !((configured >> dev) & 1ull))
     {
-      cudaError_t e = cudaFuncSetAttribute(stage_kernel<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           SH::SMEM);
+      e = cudaFuncSetAttribute(stage_kernel<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, SH::SMEM);
       if (e != cudaSuccess)
         return e;
-      configured = true;
+      if (dev < 64)
+        configured |= 1ull << dev;
     }
   const long long blocks = (args.n_cells + SH::C - 1) / SH::C;
   stage_kernel<N, T><<<(unsigned)blocks, SH::THREADS, SH::SMEM, stream>>>(args);
