@@ -138,20 +138,25 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
       phlo       = fma(-sk * (Plo + Mlo), ulo, phlo);
       phhi       = fma(sk * (Phi + Mhi), uhi, phhi);
     }
-  T w[N];
-  if (A.uniform)
-    {
+  // volume term: (1 - skew) (a u, grad v) - skew (a . grad u, v)
+  // (advection_solver.cc:500-507); with vt = det J J^{-1} a per Gauss point
+  T vtv[N], w[N];
 #pragma unroll
-      for (int q = 0; q < N; ++q)
-        w[q] = U[q];
-    }
-  else
+  for (int q = 0; q < N; ++q)
     {
-#pragma unroll
-      for (int q = 0; q < N; ++q)
-        w[q] = __ldg(vt + q * vstride) * U[q];
+      vtv[q] = A.uniform ? T(1) : __ldg(vt + q * vstride);
+      w[q]   = vtv[q] * U[q];
     }
   sweep<N, T>(tb.Dw, w, out);
+  if (A.has_skew)
+    {
+      const T sk = Consts<T>::skew(A), oms = T(1) - sk;
+      T       du[N];
+      sweep<N, T>(tb.D, U, du);
+#pragma unroll
+      for (int q = 0; q < N; ++q)
+        out[q] = fma(oms, out[q], -sk * vtv[q] * du[q]);
+    }
   const T cv = Consts<T>::cv(A, D);
 #pragma unroll
   for (int q = 0; q < N; ++q)
