@@ -12,12 +12,12 @@ cudaError_t launch_stage_fp32(int n, const StageArgs &args, cudaStream_t stream)
 {
   switch (n)
     {
-      case 2: return launch_stage_t<2, float>(args, stream);
-      case 3: return launch_stage_t<3, float>(args, stream);
-      case 4: return launch_stage_t<4, float>(args, stream);
-      case 5: return launch_stage_t<5, float>(args, stream);
-      case 6: return launch_stage_t<6, float>(args, stream);
-      case 7: return launch_stage_t<7, float>(args, stream);
+      case 2: return launch_stage_n<2, float>(args, stream);
+      case 3: return launch_stage_n<3, float>(args, stream);
+      case 4: return launch_stage_n<4, float>(args, stream);
+      case 5: return launch_stage_n<5, float>(args, stream);
+      case 6: return launch_stage_n<6, float>(args, stream);
+      case 7: return launch_stage_n<7, float>(args, stream);
       default: return cudaErrorInvalidValue;
     }
 }
@@ -26,12 +26,12 @@ int stage_cells_per_block_fp32(int n)
 {
   switch (n)
     {
-      case 2: return StageShape<2, float>::C;
-      case 3: return StageShape<3, float>::C;
-      case 4: return StageShape<4, float>::C;
-      case 5: return StageShape<5, float>::C;
-      case 6: return StageShape<6, float>::C;
-      case 7: return StageShape<7, float>::C;
+      case 2: return stage_cells<2, float>();
+      case 3: return stage_cells<3, float>();
+      case 4: return stage_cells<4, float>();
+      case 5: return stage_cells<5, float>();
+      case 6: return stage_cells<6, float>();
+      case 7: return stage_cells<7, float>();
       default: return 0;
     }
 }

@@ -12,12 +12,12 @@ cudaError_t launch_stage_fp64(int n, const StageArgs &args, cudaStream_t stream)
 {
   switch (n)
     {
-      case 2: return launch_stage_t<2, double>(args, stream);
-      case 3: return launch_stage_t<3, double>(args, stream);
-      case 4: return launch_stage_t<4, double>(args, stream);
-      case 5: return launch_stage_t<5, double>(args, stream);
-      case 6: return launch_stage_t<6, double>(args, stream);
-      case 7: return launch_stage_t<7, double>(args, stream);
+      case 2: return launch_stage_n<2, double>(args, stream);
+      case 3: return launch_stage_n<3, double>(args, stream);
+      case 4: return launch_stage_n<4, double>(args, stream);
+      case 5: return launch_stage_n<5, double>(args, stream);
+      case 6: return launch_stage_n<6, double>(args, stream);
+      case 7: return launch_stage_n<7, double>(args, stream);
       default: return cudaErrorInvalidValue;
     }
 }
@@ -26,12 +26,12 @@ int stage_cells_per_block_fp64(int n)
 {
   switch (n)
     {
-      case 2: return StageShape<2, double>::C;
-      case 3: return StageShape<3, double>::C;
-      case 4: return StageShape<4, double>::C;
-      case 5: return StageShape<5, double>::C;
-      case 6: return StageShape<6, double>::C;
-      case 7: return StageShape<7, double>::C;
+      case 2: return stage_cells<2, double>();
+      case 3: return stage_cells<3, double>();
+      case 4: return stage_cells<4, double>();
+      case 5: return stage_cells<5, double>();
+      case 6: return stage_cells<6, double>();
+      case 7: return stage_cells<7, double>();
       default: return 0;
     }
 }

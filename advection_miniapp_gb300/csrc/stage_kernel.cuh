@@ -31,21 +31,21 @@
 
 namespace adv
 {
-template <int N, typename T>
+template <int N, typename T, bool UNI>
 struct StageShape
 {
-  static constexpr int cells()
-  {
-    if (sizeof(T) == 8)
-      return N == 2 ? 32 : N == 3 ? 32 : N == 4 ? 16 : N == 5 ? 16 : N == 6 ? 8 : 8;
-    return N == 2 ? 64 : N == 3 ? 32 : N == 4 ? 32 : N == 5 ? 32 : N == 6 ? 16 : 16;
-  }
+  // cells per CTA: about 128 (or 256) threads with few idle lanes, so that
+  // several CTAs share an SM and their load and compute phases overlap
+  static constexpr int cells() { return N == 2 ? 32 : N == 3 ? 14 : N == 4 ? 8 : N == 5 ? 5 : N == 6 ? 7 : 5; }
   static constexpr int C       = cells();
   static constexpr int NQ      = N * N * N;
   static constexpr int NF      = N * N;
   static constexpr int WORK    = C * NF;
   static constexpr int THREADS = ((WORK + 31) / 32) * 32;
-  static constexpr int SMEM    = (2 * NQ + 6 * NF) * C * (int)sizeof(T) + 2 * 6 * C * (int)sizeof(int);
+  // shared memory (values of T): Ub, Qb [C][NQ]; Nb [C][6][NF]; field case:
+  // Gb [C][4][NQ] cell geometry, Fb [C][6][2][NF] face coefficients
+  static constexpr int VALUES = 2 * C * NQ + 6 * C * NF + (UNI ? 0 : 4 * C * NQ + 12 * C * NF);
+  static constexpr int SMEM   = VALUES * (int)sizeof(T) + 12 * C * (int)sizeof(int);
 };
 
 // index of the point with coordinate a along direction d and (b, c) along
@@ -91,11 +91,13 @@ __device__ __forceinline__ void sweep(const T (&M)[kMaxNDev][kMaxNDev], const T 
 }
 
 // Face terms and volume term of one direction d for one pencil of Gauss-point
-// values U along d; returns the pencil's contribution to Z (without idet).
-template <int N, typename T, int D>
+// values U along d; returns the pencil's contribution to Z (without 1/det J).
+// Flo / Fhi: [P | M] coefficients of the low / high face (field case);
+// vt: det J (J^{-1} a)_d along the pencil (field case).
+template <int N, typename T, bool UNI, int D>
 __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTables<T> &tb,
-                                               const T (&U)[N], T nlo, T nhi, int fq, int flo,
-                                               int fhi, const T *vt, int vstride, T (&out)[N])
+                                               const T (&U)[N], T nlo, T nhi, int fq, const T *Flo,
+                                               const T *Fhi, const T *vt, int vstride, T (&out)[N])
 {
   constexpr int NF = N * N;
   T             ulo = tb.l0[0] * U[0], uhi = tb.l1[0] * U[0];
@@ -106,18 +108,15 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
       uhi = fma(tb.l1[q], U[q], uhi);
     }
   T Plo, Mlo, Phi, Mhi;
-  if (A.uniform)
+  if (UNI)
     {
       Plo = Phi = Consts<T>::P(A, D);
       Mlo = Mhi = Consts<T>::M(A, D);
     }
   else
     {
-      const T *F = static_cast<const T *>(A.face_geo[D]);
-      Plo        = __ldg(F + (size_t)flo * 2 * NF + fq);
-      Mlo        = __ldg(F + (size_t)flo * 2 * NF + NF + fq);
-      Phi        = __ldg(F + (size_t)fhi * 2 * NF + fq);
-      Mhi        = __ldg(F + (size_t)fhi * 2 * NF + NF + fq);
+      Plo = Flo[fq], Mlo = Flo[NF + fq];
+      Phi = Fhi[fq], Mhi = Fhi[NF + fq];
     }
   if (A.swap_pm)
     {
@@ -129,7 +128,8 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
   // numerical flux from the cell's point of view (outward normal):
   //   low face (cell is the "plus" side):  phi = M u_own + P u_nbr
   //   high face (cell is the "minus" side): phi = -P u_own - M u_nbr
-  // plus the skew-symmetric correction +-skew c u_own, c = P + M
+  // plus the skew-symmetric correction -+ skew c u_own, c = P + M
+  // (advection_solver.cc:554-574, 615-626)
   T phlo = fma(Mlo, ulo, Plo * nlo);
   T phhi = -fma(Phi, uhi, Mhi * nhi);
   if (A.has_skew)
@@ -144,8 +144,8 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
 #pragma unroll
   for (int q = 0; q < N; ++q)
     {
-      vtv[q] = A.uniform ? T(1) : __ldg(vt + q * vstride);
-      w[q]   = vtv[q] * U[q];
+      vtv[q] = UNI ? T(1) : vt[q * vstride];
+      w[q]   = UNI ? U[q] : vtv[q] * U[q];
     }
   sweep<N, T>(tb.Dw, w, out);
   if (A.has_skew)
@@ -155,33 +155,35 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
       sweep<N, T>(tb.D, U, du);
 #pragma unroll
       for (int q = 0; q < N; ++q)
-        out[q] = fma(oms, out[q], -sk * vtv[q] * du[q]);
+        out[q] = fma(oms, out[q], -sk * (UNI ? du[q] : vtv[q] * du[q]));
     }
   const T cv = Consts<T>::cv(A, D);
 #pragma unroll
   for (int q = 0; q < N; ++q)
     {
-      T o = A.uniform ? cv * out[q] : out[q];
-      o   = fma(tb.lw0[q], phlo, o);
+      T o    = UNI ? cv * out[q] : out[q];
+      o      = fma(tb.lw0[q], phlo, o);
       out[q] = fma(tb.lw1[q], phhi, o);
     }
 }
 
-template <int N, typename T>
-__global__ void __launch_bounds__(StageShape<N, T>::THREADS)
+template <int N, typename T, bool UNI>
+__global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
   stage_kernel(const StageArgs A)
 {
-  using SH                = StageShape<N, T>;
-  constexpr int C         = SH::C;
-  constexpr int NQ        = SH::NQ;
-  constexpr int NF        = SH::NF;
-  constexpr int NT        = SH::THREADS;
+  using SH         = StageShape<N, T, UNI>;
+  constexpr int C  = SH::C;
+  constexpr int NQ = SH::NQ;
+  constexpr int NF = SH::NF;
+  constexpr int NT = SH::THREADS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T   *Ub     = reinterpret_cast<T *>(smem_raw); // [C][NQ] nodal -> Gauss values
   T   *Qb     = Ub + C * NQ;                     // [C][NQ] accumulated Z, then k
   T   *Nb     = Qb + C * NQ;                     // [C][6][NF] neighbour face values
-  int *s_nbr  = reinterpret_cast<int *>(Nb + C * 6 * NF); // [C][6] neighbour cell or -1
-  int *s_face = s_nbr + C * 6;                            // [C][6] face id
+  T   *Gb     = Nb + C * 6 * NF;                 // field: [C][4][NQ] cell geometry
+  T   *Fb     = Gb + (UNI ? 0 : C * 4 * NQ);     // field: [C][6][2][NF] face coefficients
+  int *s_nbr  = reinterpret_cast<int *>(Fb + (UNI ? 0 : C * 12 * NF)); // [C][6] neighbour or -1
+  int *s_face = s_nbr + C * 6;                                          // [C][6] face id
 
   const DevTables<T> &tb    = tab<T>(N);
   const int           tid   = threadIdx.x;
@@ -219,7 +221,8 @@ __global__ void __launch_bounds__(StageShape<N, T>::THREADS)
     }
   __syncthreads();
 
-  // ---- phase 0b: own values and the neighbours' nodal face layers
+  // ---- phase 0b: own values, the neighbours' nodal face layers and, for
+  //      curved meshes or variable velocity, the geometry (coalesced loads)
   {
     const double *src = A.r_in + cell0 * NQ;
     for (int i = tid; i < ncell * NQ; i += NT)
@@ -234,14 +237,27 @@ __global__ void __launch_bounds__(StageShape<N, T>::THREADS)
           v = from_double<T>(__ldg(A.r_in + (long long)nb * NQ + idx3<N>(d, s ? 0 : N - 1, e % N, e / N)));
         Nb[i] = v;
       }
+    if (!UNI)
+      {
+        const T *geo = static_cast<const T *>(A.cell_geo) + cell0 * 4 * NQ;
+        for (int i = tid; i < ncell * 4 * NQ; i += NT)
+          Gb[i] = __ldg(geo + i);
+        for (int i = tid; i < ncell * 12 * NF; i += NT)
+          {
+            const int cf = i / (2 * NF), e = i % (2 * NF);
+            const int d  = (cf % 6) >> 1;
+            const T  *F  = static_cast<const T *>(d == 0 ? A.face_geo[0] : d == 1 ? A.face_geo[1] : A.face_geo[2]);
+            Fb[i]        = __ldg(F + (size_t)s_face[cf] * 2 * NF + e);
+          }
+      }
   }
   __syncthreads();
 
   // ---- phase 1: S along z; neighbour layers: S along the first tangential direction
   for (int w = tid; w < ncell * NF; w += NT)
     {
-      T  *p = Ub + (w / NF) * NQ + (w % NF);
-      T   in[N], out[N];
+      T *p = Ub + (w / NF) * NQ + (w % NF);
+      T  in[N], out[N];
 #pragma unroll
       for (int k = 0; k < N; ++k)
         in[k] = p[k * NF];
@@ -302,8 +318,9 @@ __global__ void __launch_bounds__(StageShape<N, T>::THREADS)
               double g = 0.0;
               if (A.bc_exact)
                 {
-                  const double *x = A.face_x[d] + ((size_t)s_face[cf] * NF + q1 + N * k) * 3;
-                  g               = exact_value(A.ex, x[0], x[1], x[2], A.t);
+                  const double *fx = d == 0 ? A.face_x[0] : d == 1 ? A.face_x[1] : A.face_x[2];
+                  const double *x  = fx + ((size_t)s_face[cf] * NF + q1 + N * k) * 3;
+                  g                = exact_value(A.ex, x[0], x[1], x[2], A.t);
                 }
               p[k * N] = from_double<T>(g);
             }
@@ -324,10 +341,9 @@ __global__ void __launch_bounds__(StageShape<N, T>::THREADS)
 #pragma unroll
       for (int k = 0; k < N; ++k)
         p[k] = U[k];
-      const T *vt = A.uniform ? nullptr
-                              : static_cast<const T *>(A.cell_geo) + (cell0 + cl) * 4 * NQ + N * r;
-      direction_pass<N, T, 0>(A, tb, U, Nb[(cl * 6 + 0) * NF + r], Nb[(cl * 6 + 1) * NF + r], r,
-                              s_face[cl * 6 + 0], s_face[cl * 6 + 1], vt, 1, out);
+      const T *F = Fb + cl * 12 * NF;
+      direction_pass<N, T, UNI, 0>(A, tb, U, Nb[(cl * 6 + 0) * NF + r], Nb[(cl * 6 + 1) * NF + r], r,
+                                   F, F + 2 * NF, Gb + cl * 4 * NQ + N * r, 1, out);
       T *z = Qb + cl * NQ + N * r;
 #pragma unroll
       for (int k = 0; k < N; ++k)
@@ -345,10 +361,9 @@ __global__ void __launch_bounds__(StageShape<N, T>::THREADS)
 #pragma unroll
       for (int k = 0; k < N; ++k)
         U[k] = p[k * N];
-      const T *vt = A.uniform ? nullptr
-                              : static_cast<const T *>(A.cell_geo) + ((cell0 + cl) * 4 + 1) * NQ + off;
-      direction_pass<N, T, 1>(A, tb, U, Nb[(cl * 6 + 2) * NF + r], Nb[(cl * 6 + 3) * NF + r], r,
-                              s_face[cl * 6 + 2], s_face[cl * 6 + 3], vt, N, out);
+      const T *F = Fb + cl * 12 * NF + 4 * NF;
+      direction_pass<N, T, UNI, 1>(A, tb, U, Nb[(cl * 6 + 2) * NF + r], Nb[(cl * 6 + 3) * NF + r], r,
+                                   F, F + 2 * NF, Gb + (cl * 4 + 1) * NQ + off, N, out);
       T *z = Qb + cl * NQ + off;
 #pragma unroll
       for (int k = 0; k < N; ++k)
@@ -365,17 +380,17 @@ __global__ void __launch_bounds__(StageShape<N, T>::THREADS)
 #pragma unroll
       for (int k = 0; k < N; ++k)
         U[k] = p[k * NF];
-      const T *geo = A.uniform ? nullptr : static_cast<const T *>(A.cell_geo) + (cell0 + cl) * 4 * NQ;
-      direction_pass<N, T, 2>(A, tb, U, Nb[(cl * 6 + 4) * NF + r], Nb[(cl * 6 + 5) * NF + r], r,
-                              s_face[cl * 6 + 4], s_face[cl * 6 + 5], geo ? geo + 2 * NQ + r : nullptr,
-                              NF, out);
+      const T *F = Fb + cl * 12 * NF + 8 * NF;
+      const T *G = Gb + cl * 4 * NQ;
+      direction_pass<N, T, UNI, 2>(A, tb, U, Nb[(cl * 6 + 4) * NF + r], Nb[(cl * 6 + 5) * NF + r], r,
+                                   F, F + 2 * NF, G + 2 * NQ + r, NF, out);
       T *z = Qb + cl * NQ + r;
 #pragma unroll
       for (int k = 0; k < N; ++k)
         {
           zz[k] = z[k * NF] + out[k];
-          if (!A.uniform)
-            zz[k] *= __ldg(geo + 3 * NQ + r + k * NF);
+          if (!UNI)
+            zz[k] *= G[3 * NQ + r + k * NF];
         }
       sweep<N, T>(tb.Si, zz, kk);
 #pragma unroll
@@ -400,50 +415,50 @@ __global__ void __launch_bounds__(StageShape<N, T>::THREADS)
     }
   __syncthreads();
 
-  // ---- phase 7: S^-1 along x, then the Runge-Kutta update from registers
+  // ---- phase 7: S^-1 along x
   for (int w = tid; w < ncell * NF; w += NT)
     {
-      const int cl = w / NF, r = w % NF;
-      const T  *p  = Qb + cl * NQ + N * r;
-      T         in[N], kk[N];
+      T *p = Qb + (w / NF) * NQ + N * (w % NF);
+      T  in[N], out[N];
 #pragma unroll
       for (int k = 0; k < N; ++k)
         in[k] = p[k];
-      sweep<N, T>(tb.Si, in, kk);
-      const long long g = (cell0 + cl) * NQ + N * r;
-      if (A.mode == kModeApply)
-        {
+      sweep<N, T>(tb.Si, in, out);
 #pragma unroll
-          for (int k = 0; k < N; ++k)
-            A.r_out[g + k] = A.out_scale * to_double<T>(kk[k]);
-        }
-      else if (A.mode == kModeStage)
+      for (int k = 0; k < N; ++k)
+        p[k] = out[k];
+    }
+  __syncthreads();
+
+  // ---- phase 8: Runge-Kutta update over the CTA's contiguous DoF range
+  //      (the post-operation lambda of advection_solver.cc:728-752)
+  const long long g0 = cell0 * NQ;
+  if (A.mode == kModeApply)
+    {
+      for (int i = tid; i < ncell * NQ; i += NT)
+        A.r_out[g0 + i] = A.out_scale * to_double<T>(Qb[i]);
+    }
+  else if (A.mode == kModeStage)
+    {
+      for (int i = tid; i < ncell * NQ; i += NT)
         {
-#pragma unroll
-          for (int k = 0; k < N; ++k)
-            {
-              const double kd = to_double<T>(kk[k]);
-              const double u  = __ldcs(A.u_in + g + k);
-              A.u_out[g + k]  = fma(A.b, kd, u);
-              A.r_out[g + k]  = fma(A.a, kd, u);
-            }
+          const double kd = to_double<T>(Qb[i]);
+          const double u  = __ldcs(A.u_in + g0 + i);
+          A.u_out[g0 + i] = fma(A.b, kd, u);
+          A.r_out[g0 + i] = fma(A.a, kd, u);
         }
-      else
-        {
-#pragma unroll
-          for (int k = 0; k < N; ++k)
-            {
-              const double kd = to_double<T>(kk[k]);
-              A.u_out[g + k]  = fma(A.b, kd, __ldcs(A.u_in + g + k));
-            }
-        }
+    }
+  else
+    {
+      for (int i = tid; i < ncell * NQ; i += NT)
+        A.u_out[g0 + i] = fma(A.b, to_double<T>(Qb[i]), __ldcs(A.u_in + g0 + i));
     }
 }
 
-template <int N, typename T>
+template <int N, typename T, bool UNI>
 cudaError_t launch_stage_t(const StageArgs &args, cudaStream_t stream)
 {
-  using SH = StageShape<N, T>;
+  using SH = StageShape<N, T, UNI>;
   // the shared-memory opt-in is a per-device function attribute
   static unsigned long long configured = 0;
   int                       dev        = 0;
@@ -452,14 +467,26 @@ cudaError_t launch_stage_t(const StageArgs &args, cudaStream_t stream)
     return e;
   if (dev >= 64 || !((configured >> dev) & 1ull))
     {
-      e = cudaFuncSetAttribute(stage_kernel<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, SH::SMEM);
+      e = cudaFuncSetAttribute(stage_kernel<N, T, UNI>, cudaFuncAttributeMaxDynamicSharedMemorySize, SH::SMEM);
       if (e != cudaSuccess)
         return e;
       if (dev < 64)
         configured |= 1ull << dev;
     }
   const long long blocks = (args.n_cells + SH::C - 1) / SH::C;
-  stage_kernel<N, T><<<(unsigned)blocks, SH::THREADS, SH::SMEM, stream>>>(args);
+  stage_kernel<N, T, UNI><<<(unsigned)blocks, SH::THREADS, SH::SMEM, stream>>>(args);
   return cudaGetLastError();
+}
+
+template <int N, typename T>
+cudaError_t launch_stage_n(const StageArgs &args, cudaStream_t stream)
+{
+  return args.uniform ? launch_stage_t<N, T, true>(args, stream) : launch_stage_t<N, T, false>(args, stream);
+}
+
+template <int N, typename T>
+int stage_cells()
+{
+  return StageShape<N, T, true>::C;
 }
 } // namespace adv

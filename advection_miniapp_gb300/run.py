@@ -1,0 +1,106 @@
+"""Command-line driver: the counterpart of the reference's AdvectionProblem::run
+and main() (advection_solver.cc:1246-1318, 1323-1372).
+
+    python -m advection_miniapp_gb300.run --mesh deformed --cells 64 --degree 4 \
+        --steps 100 --precision fp64 [--output-every 20]
+
+Builds the operator (reinit), sets the time step by the reference's rule
+(Courant number / k^1.5, advection_solver.cc:1155-1167), projects the initial
+data, runs the low-storage Runge-Kutta loop and prints the relative L2 error,
+mass, energy and H1 seminorm at the output steps, then the time per step and
+per element like the reference's summary (advection_solver.cc:1302-1311).
+"""
+import argparse
+import json
+import time
+
+import torch
+
+from . import (AdvectionOperation, IC_BLOB, IC_SINE_GAUSS, IC_WAVE, LSRK_3_3, LSRK_5_4, LSRK_7_4, LSRK_9_5,
+               LowStorageRungeKuttaIntegrator, MESH_CARTESIAN, MESH_DEFORMED, PRECISION_FP32_OPERATOR,
+               PRECISION_FP64, make_config)
+
+SCHEMES = {"3_3": LSRK_3_3, "5_4": LSRK_5_4, "7_4": LSRK_7_4, "9_5": LSRK_9_5}
+ICS = {"sine-gauss": IC_SINE_GAUSS, "blob": IC_BLOB, "wave": IC_WAVE}
+
+
+def parse(argv=None):
+    p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("--mesh", choices=["cartesian", "deformed"], default="cartesian")
+    p.add_argument("--cells", type=int, default=8, help="cells per direction")
+    p.add_argument("--degree", type=int, default=3)
+    p.add_argument("--deformation", type=float, default=0.08)
+    p.add_argument("--velocity", type=float, nargs=3, default=(1.0, 0.15, -0.05))
+    p.add_argument("--initial-condition", choices=sorted(ICS), default="sine-gauss")
+    p.add_argument("--courant", type=float, default=0.5)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--scheme", choices=sorted(SCHEMES), default="5_4")
+    p.add_argument("--precision", choices=["fp64", "fp32"], default="fp64")
+    p.add_argument("--flux-alpha", type=float, default=1.0)
+    p.add_argument("--skew", type=float, default=0.0)
+    p.add_argument("--output-every", type=int, default=0, help="0: only at the start and the end")
+    p.add_argument("--json", action="store_true", help="print one JSON summary line")
+    return p.parse_args(argv)
+
+
+def main(argv=None):
+    args = parse(argv)
+    cfg = make_config(degree=args.degree, n_cells=(args.cells,) * 3,
+                      mesh_type=MESH_DEFORMED if args.mesh == "deformed" else MESH_CARTESIAN,
+                      deformation=args.deformation if args.mesh == "deformed" else 0.0,
+                      velocity=tuple(args.velocity), initial_condition=ICS[args.initial_condition],
+                      flux_alpha=args.flux_alpha, factor_skew=args.skew,
+                      precision=PRECISION_FP64 if args.precision == "fp64" else PRECISION_FP32_OPERATOR)
+    op = AdvectionOperation(cfg)
+    integ = LowStorageRungeKuttaIntegrator(SCHEMES[args.scheme])
+    dt = op.time_step(args.courant)
+    if not args.json:
+        print(f"   Number of elements:            {op.n_cells}")
+        print(f"   Polynomial degree:             {op.degree}")
+        print(f"   Number of degrees of freedom:  {op.n_dofs}")
+        print(f"   Time step size: {dt:.6g}")
+    u = op.initialize_dof_vector()
+    op.project_initial(u)
+    r, k = op.initialize_dof_vector(), op.initialize_dof_vector()
+
+    def output(step, t):
+        err, nrm = op.l2_error(u, t)
+        me = op.compute_mass_and_energy(u)
+        if not args.json:
+            print(f"   Time {t:8.3g}  error {err / nrm:10.5g}  mass {me[0]:16.10g}  energy {me[1]:16.10g}"
+                  f"  H1-semi {me[2]:9.4g}")
+        return err / nrm, me
+
+    output(0, 0.0)
+    t = 0.0
+    wall = 0.0
+    step = 0
+    chunk = args.output_every if args.output_every > 0 else args.steps
+    while step < args.steps:
+        n = min(chunk, args.steps - step)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if n == 1:
+            integ.perform_time_step(op, t, dt, u, r, k)
+        else:
+            op.lsrk_steps(integ.scheme, t, dt, n, u, r, k)
+        torch.cuda.synchronize()
+        wall += time.perf_counter() - t0
+        step += n
+        t = step * dt
+        if args.output_every > 0 or step == args.steps:
+            rel, me = output(step, t)
+    per_step = wall / max(args.steps, 1)
+    stage_rate = op.n_dofs * integ.n_stages() * args.steps / wall / 1e9 if wall > 0 else 0.0
+    if args.json:
+        print(json.dumps({"n_dofs": op.n_dofs, "steps": args.steps, "dt": dt, "t_end": t, "rel_l2_error": rel,
+                          "mass_energy": list(me), "s_per_step": per_step, "gdofs_per_stage": stage_rate}))
+    else:
+        print(f"\n   Performed {args.steps} time steps.")
+        print(f"   Average wall clock time per time step: {per_step:.4g}s, time per element: "
+              f"{per_step / op.n_cells:.4g}s")
+        print(f"   Throughput: {stage_rate:.4g} GDoF/s per Runge-Kutta stage")
+
+
+if __name__ == "__main__":
+    main()
