@@ -78,5 +78,23 @@ def build(verbose=False, force=False):
     return LIB_PATH
 
 
+DRIVER_SRC = os.path.join(HERE, "cpp", "advection_solver.cpp")
+DRIVER_BIN = os.path.join(BUILD_DIR, "advection_solver")
+
+
+def build_driver():
+    """Compile the C++ driver program (cpp/advection_solver.cpp) against the library."""
+    lib = build()
+    deps = [DRIVER_SRC, lib, os.path.join(os.path.dirname(HERE), "include", "advection_gb300.hpp")]
+    if os.path.exists(DRIVER_BIN) and os.path.getmtime(DRIVER_BIN) >= _newest(deps):
+        return DRIVER_BIN
+    cmd = [nvcc(), "-O2", "-std=c++17", "-I", os.path.join(os.path.dirname(HERE), "include"), DRIVER_SRC,
+           "-o", DRIVER_BIN, "-L", HERE, "-ladvection_gb300", "-Xlinker", "-rpath," + HERE]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
+    return DRIVER_BIN
+
+
 if __name__ == "__main__":
     print(build(verbose=True, force="--force" in sys.argv))
