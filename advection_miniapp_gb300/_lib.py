@@ -73,6 +73,7 @@ SIGNATURES = {
     "adv_copy_from_host": (_I, [_P, _P, _P, _P]),
     "adv_launch_count": (_I, [_P, ctypes.POINTER(_I64)]),
     "adv_measure_fma_peak": (_I, [_I, _DP, _P]),
+    "adv_perform_stage_noalloc": (_I, [_P, _D, _D, _D, _P, _P, _P, _P, _P]),
 }
 
 _lib = None

@@ -722,6 +722,85 @@ int adv_measure_fma_peak(int precision, double *tflops, void *stream)
 
 } // extern "C"
 
+// ---------------------------------------------------------------------------
+// Allocation-free stage (adv_perform_stage_noalloc).  Callers that cannot
+// allocate device memory mid-solve (memory-budgeted serving, latency-critical
+// loops, memory owned by another allocator) get the staging buffer for an
+// output that aliases r_in from this file-scope array instead of a
+// handle-owned vector.  Host code must not take the array's address
+// directly (in host code the name is a host-side shadow, not a device
+// address): noalloc_scratch() looks up the device address once per device
+// with that device current.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) double g_noalloc_stage_scratch[ADV_NOALLOC_MAX_DOFS];
+
+namespace
+{
+std::mutex g_noalloc_mutex;
+double    *g_noalloc_ptr[256] = {};
+
+int noalloc_scratch(int device, double **out)
+{
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (device < 0 || device >= 256)
+    return fail(ADV_ERR_INVALID, "device index out of range");
+  if (!g_noalloc_ptr[device])
+    {
+      void       *p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_stage_scratch);
+      if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGetSymbolAddress of the static stage scratch");
+      g_noalloc_ptr[device] = static_cast<double *>(p);
+    }
+  *out = g_noalloc_ptr[device];
+  return ADV_OK;
+}
+} // namespace
+
+extern "C" int adv_perform_stage_noalloc(adv_handle *h, double t, double b_dt, double a_dt,
+                                         const double *r_in, double *k, double *u, double *r_out,
+                                         void *stream)
+{
+  (void)k; // scratch in the reference's semantics; this variant does not need it
+  if (!h || !r_in || !u || (a_dt != 0.0 && !r_out))
+    return fail(ADV_ERR_INVALID, "null argument");
+  if (a_dt != 0.0 && r_out == u)
+    return fail(ADV_ERR_ALIASING, "r_out must not alias u");
+  if (h->mesh.n_dofs > (int64_t)ADV_NOALLOC_MAX_DOFS)
+    return fail(ADV_ERR_INVALID, "adv_perform_stage_noalloc: the mesh has " + std::to_string(h->mesh.n_dofs) +
+                                   " DoFs, more than the static scratch of ADV_NOALLOC_MAX_DOFS = " +
+                                   std::to_string((long long)ADV_NOALLOC_MAX_DOFS) +
+                                   "; use adv_perform_stage");
+  if (int e = check_device(h))
+    return e;
+  double *scratch = nullptr;
+  if (int e = noalloc_scratch(h->device, &scratch))
+    return e;
+  cudaStream_t   s   = (cudaStream_t)stream;
+  const size_t   nb  = h->mesh.n_dofs * sizeof(double);
+  adv::StageArgs A   = base_args(*h, t);
+  const double   fac = A.out_scale;
+  A.r_in             = r_in;
+  A.u_in             = u;
+  A.b                = b_dt * fac;
+  A.a                = a_dt * fac;
+  A.mode             = a_dt == 0.0 ? adv::kModeLastStage : adv::kModeStage;
+  // an output aliasing r_in (read by neighbouring cells during the kernel) is
+  // staged in the static array; u == r_in and r_out == r_in cannot both hold
+  // because r_out == u is rejected above
+  double *u_target = u == r_in ? scratch : u;
+  double *r_target = (a_dt != 0.0 && r_out == r_in) ? scratch : r_out;
+  A.u_out          = u_target;
+  A.r_out          = a_dt != 0.0 ? r_target : nullptr;
+  if (int e = launch(h, A, s))
+    return e;
+  if (u_target != u)
+    ADV_CUDA(cudaMemcpyAsync(u, u_target, nb, cudaMemcpyDeviceToDevice, s));
+  if (a_dt != 0.0 && r_target != r_out)
+    ADV_CUDA(cudaMemcpyAsync(r_out, r_target, nb, cudaMemcpyDeviceToDevice, s));
+  return ADV_OK;
+}
+
 namespace adv
 {
 cudaError_t launch_stage(int n, int precision, const StageArgs &args, cudaStream_t stream)
