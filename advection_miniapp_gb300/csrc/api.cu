@@ -67,6 +67,30 @@ int cuda_fail(cudaError_t e, const char *where)
 std::mutex g_table_mutex;
 bool       g_tables_uploaded[256] = {};
 
+// even-odd form of a reflection-(anti)symmetric n x n matrix M[q][i]
+template <typename T>
+void even_odd(int n, const double (&M)[adv::kMaxN][adv::kMaxN], bool anti, adv::EvenOdd<T> &eo)
+{
+  const int h = n / 2;
+  std::memset(&eo, 0, sizeof(eo));
+  for (int q = 0; q < h; ++q)
+    {
+      for (int i = 0; i < h; ++i)
+        {
+          eo.e[q][i] = (T)(0.5 * (M[q][i] + M[q][n - 1 - i]));
+          eo.o[q][i] = (T)(0.5 * (M[q][i] - M[q][n - 1 - i]));
+        }
+      if (n % 2)
+        eo.ce[q] = (T)M[q][h];
+    }
+  if (n % 2)
+    {
+      for (int i = 0; i < h; ++i)
+        eo.mid[i] = (T)M[h][i];
+      eo.cc = anti ? (T)0 : (T)M[h][h];
+    }
+}
+
 int ensure_tables(int device)
 {
   std::lock_guard<std::mutex> lock(g_table_mutex);
@@ -100,6 +124,18 @@ int ensure_tables(int device)
           tf[n].l0[q] = (float)t.l0[q], tf[n].l1[q] = (float)t.l1[q];
           tf[n].lw0[q] = (float)t.lw0[q], tf[n].lw1[q] = (float)t.lw1[q], tf[n].gw[q] = (float)t.gw[q];
         }
+      double Si[adv::kMaxN][adv::kMaxN] = {};
+      for (int i = 0; i < n; ++i)
+        for (int q = 0; q < n; ++q)
+          Si[i][q] = t.Si[i][q];
+      even_odd(n, t.S, false, td[n].S_eo);
+      even_odd(n, Si, false, td[n].Si_eo);
+      even_odd(n, t.Dw, true, td[n].Dw_eo);
+      even_odd(n, t.D, true, td[n].D_eo);
+      even_odd(n, t.S, false, tf[n].S_eo);
+      even_odd(n, Si, false, tf[n].Si_eo);
+      even_odd(n, t.Dw, true, tf[n].Dw_eo);
+      even_odd(n, t.D, true, tf[n].D_eo);
     }
   ADV_CUDA(adv::upload_tables_stage64(td, tf));
   ADV_CUDA(adv::upload_tables_stage32(td, tf));

@@ -12,6 +12,20 @@ namespace adv
 {
 constexpr int kMaxNDev = 7;
 
+// Even-odd form of an n x n matrix M that is symmetric (M[n-1-q][n-1-i] =
+// M[q][i]) or antisymmetric (= -M[q][i]) under reflection of both indices:
+// with e_i = x_i + x_{n-1-i}, o_i = x_i - x_{n-1-i} (i < n/2) and the middle
+// entry c (odd n), out_q = E_q + O_q and out_{n-1-q} = E_q - O_q
+// (antisymmetric: O_q - E_q), E_q = sum e[q][i] e_i + ce[q] c,
+// O_q = sum o[q][i] o_i; the middle output is sum mid[i] e_i + cc c
+// (antisymmetric: sum mid[i] o_i).  For n = 5 a sweep costs 21 instead of 25
+// operations.
+template <typename T>
+struct EvenOdd
+{
+  T e[4][4], o[4][4], ce[4], mid[4], cc;
+};
+
 template <typename T>
 struct DevTables
 {
@@ -22,6 +36,7 @@ struct DevTables
   T l0[kMaxNDev], l1[kMaxNDev];   // Gauss-Lagrange basis at xi = 0, 1
   T lw0[kMaxNDev], lw1[kMaxNDev]; // the same divided by the Gauss weights
   T gw[kMaxNDev];                 // Gauss weights
+  EvenOdd<T> S_eo, Si_eo, Dw_eo, D_eo;  // S, S^-1 symmetric; Dw, D antisymmetric
 };
 
 // Index [n] holds the tables of n points per direction.  The library is

@@ -27,6 +27,8 @@
 // from registers into the LSRK update.
 #pragma once
 
+#include <cuda_pipeline.h>
+
 #include "kernels.h"
 
 namespace adv
@@ -90,6 +92,54 @@ __device__ __forceinline__ void sweep(const T (&M)[kMaxNDev][kMaxNDev], const T 
     }
 }
 
+// The same product through the even-odd form (fewer operations for n >= 5).
+template <int N, typename T, bool ANTI>
+__device__ __forceinline__ void sweep_eo(const EvenOdd<T> &M, const T (&in)[N], T (&out)[N])
+{
+  constexpr int H = N / 2;
+  T             e[H > 0 ? H : 1], o[H > 0 ? H : 1];
+#pragma unroll
+  for (int i = 0; i < H; ++i)
+    {
+      e[i] = in[i] + in[N - 1 - i];
+      o[i] = in[i] - in[N - 1 - i];
+    }
+#pragma unroll
+  for (int q = 0; q < H; ++q)
+    {
+      T E = M.e[q][0] * e[0], O = M.o[q][0] * o[0];
+#pragma unroll
+      for (int i = 1; i < H; ++i)
+        {
+          E = fma(M.e[q][i], e[i], E);
+          O = fma(M.o[q][i], o[i], O);
+        }
+      if (N % 2)
+        E = fma(M.ce[q], in[H], E);
+      out[q]         = E + O;
+      out[N - 1 - q] = ANTI ? O - E : E - O;
+    }
+  if (N % 2)
+    {
+      T m = ANTI ? M.mid[0] * o[0] : fma(M.mid[0], e[0], M.cc * in[H]);
+#pragma unroll
+      for (int i = 1; i < H; ++i)
+        m = fma(M.mid[i], ANTI ? o[i] : e[i], m);
+      out[H] = m;
+    }
+}
+
+// Sweep with the cheaper of the two forms: even-odd pays off from n = 5.
+template <int N, typename T, bool ANTI>
+__device__ __forceinline__ void sweep2(const T (&M)[kMaxNDev][kMaxNDev], const EvenOdd<T> &Meo,
+                                       const T (&in)[N], T (&out)[N])
+{
+  if (N >= 5)
+    sweep_eo<N, T, ANTI>(Meo, in, out);
+  else
+    sweep<N, T>(M, in, out);
+}
+
 // Face terms and volume term of one direction d for one pencil of Gauss-point
 // values U along d; returns the pencil's contribution to Z (without 1/det J).
 // Flo / Fhi: [P | M] coefficients of the low / high face (field case);
@@ -147,12 +197,12 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
       vtv[q] = UNI ? T(1) : vt[q * vstride];
       w[q]   = UNI ? U[q] : vtv[q] * U[q];
     }
-  sweep<N, T>(tb.Dw, w, out);
+  sweep2<N, T, true>(tb.Dw, tb.Dw_eo, w, out);
   if (A.has_skew)
     {
       const T sk = Consts<T>::skew(A), oms = T(1) - sk;
       T       du[N];
-      sweep<N, T>(tb.D, U, du);
+      sweep2<N, T, true>(tb.D, tb.D_eo, U, du);
 #pragma unroll
       for (int q = 0; q < N; ++q)
         out[q] = fma(oms, out[q], -sk * (UNI ? du[q] : vtv[q] * du[q]));
@@ -221,63 +271,69 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
     }
   __syncthreads();
 
-  // ---- phase 0b: own values, the neighbours' nodal face layers and, for
-  //      curved meshes or variable velocity, the geometry (coalesced loads)
+  // ---- phase 0b: curved meshes / variable velocity: start the asynchronous
+  //      copies of the cell geometry (16-byte chunks) and the face
+  //      coefficients (8-byte chunks) into shared memory; they land while the
+  //      interpolation sweeps below run
+  if (!UNI)
+    {
+      const char *geo = reinterpret_cast<const char *>(static_cast<const T *>(A.cell_geo) + cell0 * 4 * NQ);
+      const int   n16 = ncell * 4 * NQ * (int)sizeof(T) / 16;
+      for (int i = tid; i < n16; i += NT)
+        __pipeline_memcpy_async(reinterpret_cast<char *>(Gb) + 16 * i, geo + 16 * i, 16);
+      constexpr int F8 = 2 * NF * (int)sizeof(T) / 8; // 8-byte chunks per cell-face
+      for (int i = tid; i < ncell * 6 * F8; i += NT)
+        {
+          const int cf = i / F8, e = i % F8;
+          const int d  = (cf % 6) >> 1;
+          const T  *F  = static_cast<const T *>(d == 0 ? A.face_geo[0] : d == 1 ? A.face_geo[1] : A.face_geo[2]);
+          __pipeline_memcpy_async(reinterpret_cast<char *>(Fb + cf * 2 * NF) + 8 * e,
+                                  reinterpret_cast<const char *>(F + (size_t)s_face[cf] * 2 * NF) + 8 * e, 8);
+        }
+      __pipeline_commit();
+    }
+
+  // ---- phase 1: own values loaded as z-pencils and interpolated along z;
+  //      neighbour face layers loaded as rows along their first tangential
+  //      direction and interpolated along it
   {
     const double *src = A.r_in + cell0 * NQ;
-    for (int i = tid; i < ncell * NQ; i += NT)
-      Ub[i] = from_double<T>(__ldg(src + i));
-    for (int i = tid; i < ncell * 6 * NF; i += NT)
+    for (int w = tid; w < ncell * NF; w += NT)
       {
-        const int cf = i / NF, e = i % NF;
-        const int j = cf % 6, d = j >> 1, s = j & 1;
-        const int nb = s_nbr[cf];
-        T         v  = T(0);
-        if (nb >= 0)
-          v = from_double<T>(__ldg(A.r_in + (long long)nb * NQ + idx3<N>(d, s ? 0 : N - 1, e % N, e / N)));
-        Nb[i] = v;
+        const int     cl = w / NF, r = w % NF;
+        const double *g  = src + cl * NQ + r;
+        T             in[N], out[N];
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+          in[k] = from_double<T>(__ldg(g + k * NF));
+        sweep2<N, T, false>(tb.S, tb.S_eo, in, out);
+        T *p = Ub + cl * NQ + r;
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+          p[k * NF] = out[k];
       }
-    if (!UNI)
+    for (int w = tid; w < ncell * 6 * N; w += NT)
       {
-        const T *geo = static_cast<const T *>(A.cell_geo) + cell0 * 4 * NQ;
-        for (int i = tid; i < ncell * 4 * NQ; i += NT)
-          Gb[i] = __ldg(geo + i);
-        for (int i = tid; i < ncell * 12 * NF; i += NT)
-          {
-            const int cf = i / (2 * NF), e = i % (2 * NF);
-            const int d  = (cf % 6) >> 1;
-            const T  *F  = static_cast<const T *>(d == 0 ? A.face_geo[0] : d == 1 ? A.face_geo[1] : A.face_geo[2]);
-            Fb[i]        = __ldg(F + (size_t)s_face[cf] * 2 * NF + e);
-          }
+        const int cf = w / N, b = w % N;
+        const int nb = s_nbr[cf];
+        if (nb < 0)
+          continue; // boundary face: phase 2 writes the Dirichlet data
+        const int j = cf % 6, d = j >> 1, layer = (j & 1) ? 0 : N - 1;
+        // nodal index of (layer along d, a along t1, b along t2) = base + a * stride
+        const int     base   = d == 0 ? layer + NF * b : d == 1 ? N * layer + NF * b : N * b + NF * layer;
+        const int     stride = d == 0 ? N : 1;
+        const double *g      = A.r_in + (long long)nb * NQ + base;
+        T             in[N], out[N];
+#pragma unroll
+        for (int a = 0; a < N; ++a)
+          in[a] = from_double<T>(__ldg(g + a * stride));
+        sweep2<N, T, false>(tb.S, tb.S_eo, in, out);
+        T *p = Nb + cf * NF + N * b;
+#pragma unroll
+        for (int a = 0; a < N; ++a)
+          p[a] = out[a];
       }
   }
-  __syncthreads();
-
-  // ---- phase 1: S along z; neighbour layers: S along the first tangential direction
-  for (int w = tid; w < ncell * NF; w += NT)
-    {
-      T *p = Ub + (w / NF) * NQ + (w % NF);
-      T  in[N], out[N];
-#pragma unroll
-      for (int k = 0; k < N; ++k)
-        in[k] = p[k * NF];
-      sweep<N, T>(tb.S, in, out);
-#pragma unroll
-      for (int k = 0; k < N; ++k)
-        p[k * NF] = out[k];
-    }
-  for (int w = tid; w < ncell * 6 * N; w += NT)
-    {
-      T *p = Nb + (w / N) * NF + (w % N) * N;
-      T  in[N], out[N];
-#pragma unroll
-      for (int k = 0; k < N; ++k)
-        in[k] = p[k];
-      sweep<N, T>(tb.S, in, out);
-#pragma unroll
-      for (int k = 0; k < N; ++k)
-        p[k] = out[k];
-    }
   __syncthreads();
 
   // ---- phase 2: S along y; neighbour layers along the second tangential
@@ -290,7 +346,7 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
 #pragma unroll
       for (int k = 0; k < N; ++k)
         in[k] = p[k * N];
-      sweep<N, T>(tb.S, in, out);
+      sweep2<N, T, false>(tb.S, tb.S_eo, in, out);
 #pragma unroll
       for (int k = 0; k < N; ++k)
         p[k * N] = out[k];
@@ -305,7 +361,7 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
 #pragma unroll
           for (int k = 0; k < N; ++k)
             in[k] = p[k * N];
-          sweep<N, T>(tb.S, in, out);
+          sweep2<N, T, false>(tb.S, tb.S_eo, in, out);
 #pragma unroll
           for (int k = 0; k < N; ++k)
             p[k * N] = out[k];
@@ -326,6 +382,8 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
             }
         }
     }
+  if (!UNI)
+    __pipeline_wait_prior(0);
   __syncthreads();
 
   // ---- phase 3: S along x gives the Gauss-point values; x-direction terms
@@ -337,7 +395,7 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
 #pragma unroll
       for (int k = 0; k < N; ++k)
         in[k] = p[k];
-      sweep<N, T>(tb.S, in, U);
+      sweep2<N, T, false>(tb.S, tb.S_eo, in, U);
 #pragma unroll
       for (int k = 0; k < N; ++k)
         p[k] = U[k];
@@ -392,7 +450,7 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
           if (!UNI)
             zz[k] *= G[3 * NQ + r + k * NF];
         }
-      sweep<N, T>(tb.Si, zz, kk);
+      sweep2<N, T, false>(tb.Si, tb.Si_eo, zz, kk);
 #pragma unroll
       for (int k = 0; k < N; ++k)
         z[k * NF] = kk[k];
@@ -408,7 +466,7 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
 #pragma unroll
       for (int k = 0; k < N; ++k)
         in[k] = p[k * N];
-      sweep<N, T>(tb.Si, in, out);
+      sweep2<N, T, false>(tb.Si, tb.Si_eo, in, out);
 #pragma unroll
       for (int k = 0; k < N; ++k)
         p[k * N] = out[k];
@@ -423,7 +481,7 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
 #pragma unroll
       for (int k = 0; k < N; ++k)
         in[k] = p[k];
-      sweep<N, T>(tb.Si, in, out);
+      sweep2<N, T, false>(tb.Si, tb.Si_eo, in, out);
 #pragma unroll
       for (int k = 0; k < N; ++k)
         p[k] = out[k];
