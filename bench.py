@@ -62,13 +62,43 @@ def dist_env():
 # --------------------------------------------------------------------------
 # algorithmic work model of the fused stage kernel (per cell, n = k + 1)
 # --------------------------------------------------------------------------
-def fp_work_per_cell(n, curved=True):
-    """(FP instructions, flops with FMA = 2) of one fused stage per cell: three
-    interpolation sweeps, neighbour face interpolation (2 sweeps on 6 layers),
-    three direction passes (face traces, fluxes, volume derivative, lifts),
-    1/det J, three inverse-mass sweeps and the 2-FMA vector update."""
-    inst = 9 * n ** 4 + (30 if curved else 29) * n ** 3 + 12 * n ** 2
-    flops = 18 * n ** 4 + (47 if curved else 46) * n ** 3
+def _sweep_cost(n, anti):
+    """(instructions, flops) of one 1D sweep over a pencil of n values as the
+    kernel executes it: the full n x n product for n < 5, else the even-odd
+    form (sums/differences of mirrored entries, two half-size products,
+    recombination)."""
+    if n < 5:
+        return n * n, 2 * n * n - n
+    h, odd = n // 2, n % 2
+    inst = 2 * h + h * (h + odd + h + 2) + odd * (h + (0 if anti else 1))
+    flops = 2 * h + h * (4 * h + 2 * odd) + odd * (2 * h - 1 + (0 if anti else 2))
+    return inst, flops
+
+
+def fp_work_per_cell(n, curved=True, stage=True):
+    """(FP instructions, flops with FMA = 2) of one fused stage per cell,
+    phase by phase as in stage_kernel: interpolation sweeps of the own cell
+    (3 x n^2 pencils) and of the six neighbour layers (2 x 6n rows), three
+    direction passes per pencil (two face traces, flux, volume term with the
+    weighted derivative, two lifts), 1/det J, three inverse-mass sweeps and the
+    two-FMA update per DoF."""
+    si, sf = _sweep_cost(n, anti=False)
+    di, df = _sweep_cost(n, anti=True)
+    p = n * n
+    inst = 3 * p * si + 12 * n * si
+    flops = 3 * p * sf + 12 * n * sf
+    pass_i = 2 * n + 4 + (n if curved else n) + di + 2 * n
+    pass_f = 2 * (2 * n - 1) + 6 + n + df + 4 * n
+    inst += 3 * p * pass_i
+    flops += 3 * p * pass_f
+    if curved:
+        inst += n ** 3
+        flops += n ** 3
+    inst += 3 * p * si
+    flops += 3 * p * sf
+    upd = 2 if stage else 1
+    inst += upd * n ** 3
+    flops += 2 * upd * n ** 3
     return inst, flops
 
 
@@ -316,7 +346,9 @@ def ours(args):
     n = 5
     launch64 = r64["seconds"] / (STAGES * args.steps)
     launch32 = r32["seconds"] / (STAGES * args.steps)
-    inst, flops = fp_work_per_cell(n)
+    # average over the 5 launches of a step: 4 stages with 2 update FMAs per DoF, the last with 1
+    inst = (4 * fp_work_per_cell(n)[0] + fp_work_per_cell(n, stage=False)[0]) / STAGES
+    flops = (4 * fp_work_per_cell(n)[1] + fp_work_per_cell(n, stage=False)[1]) / STAGES
     vec_bytes_launch = bytes_per_dof_step() / STAGES * n_dofs
     achieved64 = flops * n_cells / launch64 / 1e12
     achieved32_hbm = vec_bytes_launch / launch32 / 1e9
@@ -355,6 +387,7 @@ def ours(args):
                      "unit": "TFLOP/s", "frac": round(achieved64 / fp64_peak, 4), "traffic": None,
                      "peak_source": "FP64 FMA microbenchmark (adv_measure_fma_peak) on this GPU",
                      "flops_per_cell": flops, "fp64_inst_per_cell": inst,
+                     "fp64_inst_frac": round(inst * n_cells / launch64 / (fp64_peak * 1e12 / 2), 4),
                      "hbm_achieved_gbs": round(vec_bytes_launch / launch64 / 1e9 + geo64, 2),
                      "hbm_frac_of_measured": round((vec_bytes_launch / launch64 / 1e9 + geo64) / hbm_peak, 4),
                      "launch_ms": round(launch64 * 1e3, 4)},
