@@ -123,6 +123,11 @@ int ensure_tables(int device)
           td[n].lw0[q] = t.lw0[q], td[n].lw1[q] = t.lw1[q], td[n].gw[q] = t.gw[q];
           tf[n].l0[q] = (float)t.l0[q], tf[n].l1[q] = (float)t.l1[q];
           tf[n].lw0[q] = (float)t.lw0[q], tf[n].lw1[q] = (float)t.lw1[q], tf[n].gw[q] = (float)t.gw[q];
+          td[n].ld0[q] = t.ld0[q], td[n].ld1[q] = t.ld1[q], td[n].lwd0[q] = t.lwd0[q], td[n].lwd1[q] = t.lwd1[q];
+          td[n].dphi0[q] = t.dphi0[q], td[n].dphi1[q] = t.dphi1[q];
+          tf[n].ld0[q] = (float)t.ld0[q], tf[n].ld1[q] = (float)t.ld1[q];
+          tf[n].lwd0[q] = (float)t.lwd0[q], tf[n].lwd1[q] = (float)t.lwd1[q];
+          tf[n].dphi0[q] = (float)t.dphi0[q], tf[n].dphi1[q] = (float)t.dphi1[q];
         }
       double Si[adv::kMaxN][adv::kMaxN] = {};
       for (int i = 0; i < n; ++i)
@@ -174,8 +179,12 @@ int validate(const adv_config &c)
     return fail(ADV_ERR_INVALID, "blob width ic_params[3] must be positive");
   if (c.precision != ADV_PRECISION_FP64 && c.precision != ADV_PRECISION_FP32_OPERATOR)
     return fail(ADV_ERR_INVALID, "unknown precision");
-  if (c.diffusion != 0.0)
-    return fail(ADV_ERR_INVALID, "diffusion (SIPG) is not available in this build");
+  if (c.diffusion < 0.0)
+    return fail(ADV_ERR_INVALID, "diffusion must be >= 0");
+  if (c.diffusion != 0.0 && c.mesh_type != ADV_MESH_CARTESIAN)
+    return fail(ADV_ERR_INVALID, "diffusion (SIPG) runs on affine meshes only");
+  if (c.diffusion != 0.0 && !(c.penalty_factor > 0.0))
+    return fail(ADV_ERR_INVALID, "penalty_factor must be positive with diffusion");
   if (!(c.flux_alpha >= 0.0 && c.flux_alpha <= 1.0))
     return fail(ADV_ERR_INVALID, "flux_alpha must be in [0, 1]");
   return ADV_OK;
@@ -276,6 +285,26 @@ adv::StageArgs base_args(const adv_handle &h, double t)
   const double s = time_factor(h, t);
   A.swap_pm      = s < 0.0;
   A.out_scale    = s;
+  if (h.cfg.diffusion != 0.0)
+    {
+      // SIPG on the affine mesh: the velocity factor is applied in the kernel
+      // (it does not scale the viscous terms), so outputs are not rescaled
+      A.visc       = 1;
+      A.adv_scale  = s;
+      A.adv_scalef = (float)s;
+      A.out_scale  = 1.0;
+      const double nu = h.cfg.diffusion, V = m.h[0] * m.h[1] * m.h[2];
+      for (int d = 0; d < 3; ++d)
+        {
+          const double sigma = h.cfg.penalty_factor * (h.cfg.degree + 1.0) * (h.cfg.degree + 1.0) / m.h[d];
+          A.K1[d]     = nu * sigma * V / m.h[d];
+          A.K2[d]     = nu * V / (2.0 * m.h[d] * m.h[d]);
+          A.cdiff[d]  = nu * V / (m.h[d] * m.h[d]);
+          A.K1f[d]    = (float)A.K1[d];
+          A.K2f[d]    = (float)A.K2[d];
+          A.cdifff[d] = (float)A.cdiff[d];
+        }
+    }
   return A;
 }
 

@@ -142,7 +142,7 @@ int setup_mesh(const adv_config &cfg, Mesh &m)
   m.n        = cfg.degree + 1;
   m.curved   = cfg.mesh_type == ADV_MESH_DEFORMED;
   m.periodic = cfg.periodic != 0;
-  m.uniform  = !m.curved && cfg.velocity_type == ADV_VELOCITY_CONSTANT;
+  m.uniform  = !m.curved && cfg.velocity_type == ADV_VELOCITY_CONSTANT && cfg.diffusion == 0.0;
   m.n_cells  = 1;
   for (int d = 0; d < 3; ++d)
     {

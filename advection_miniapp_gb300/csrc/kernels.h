@@ -39,6 +39,13 @@ struct StageArgs
   double        skew;
   float         cvf[3], Pf[3], Mf[3], skewf; // the same in binary32 for the FP32 operator
   int           has_skew;
+  int           visc;        // SIPG diffusion on an affine mesh (field geometry)
+  // SIPG constants per direction (V = cell volume, h = cell width, sigma the penalty):
+  // K1 = nu sigma V / h, K2 = nu V / (2 h^2), cdiff = nu V / h^2
+  double        K1[3], K2[3], cdiff[3];
+  float         K1f[3], K2f[3], cdifff[3];
+  double        adv_scale;   // velocity time factor, applied in-kernel when visc != 0
+  float         adv_scalef;
   int           pad1;
   const void   *cell_geo;    // field case: [vt0|vt1|vt2|idet] x n^3 per cell (T)
   const void   *face_geo[3]; // field case: [P|M] x n^2 per face (T)

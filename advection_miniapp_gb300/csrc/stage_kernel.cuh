@@ -33,7 +33,7 @@
 
 namespace adv
 {
-template <int N, typename T, bool UNI>
+template <int N, typename T, bool UNI, bool VISC = false>
 struct StageShape
 {
   // cells per CTA: about 128 (or 256) threads with few idle lanes, so that
@@ -46,7 +46,9 @@ struct StageShape
   static constexpr int THREADS = ((WORK + 31) / 32) * 32;
   // shared memory (values of T): Ub, Qb [C][NQ]; Nb [C][6][NF]; field case:
   // Gb [C][4][NQ] cell geometry, Fb [C][6][2][NF] face coefficients
-  static constexpr int VALUES = 2 * C * NQ + 6 * C * NF + (UNI ? 0 : 4 * C * NQ + 12 * C * NF);
+  // viscous terms: Nd [C][6][NF] neighbour normal derivatives at the face points
+  static constexpr int VALUES =
+    2 * C * NQ + 6 * C * NF + (UNI ? 0 : 4 * C * NQ + 12 * C * NF) + (VISC ? 6 * C * NF : 0);
   static constexpr int SMEM   = VALUES * (int)sizeof(T) + 12 * C * (int)sizeof(int);
 };
 
@@ -68,6 +70,10 @@ struct Consts<double>
   static __device__ __forceinline__ double P(const StageArgs &A, int d) { return A.P[d]; }
   static __device__ __forceinline__ double M(const StageArgs &A, int d) { return A.M[d]; }
   static __device__ __forceinline__ double skew(const StageArgs &A) { return A.skew; }
+  static __device__ __forceinline__ double K1(const StageArgs &A, int d) { return A.K1[d]; }
+  static __device__ __forceinline__ double K2(const StageArgs &A, int d) { return A.K2[d]; }
+  static __device__ __forceinline__ double cdiff(const StageArgs &A, int d) { return A.cdiff[d]; }
+  static __device__ __forceinline__ double sa(const StageArgs &A) { return A.adv_scale; }
 };
 template <>
 struct Consts<float>
@@ -76,6 +82,10 @@ struct Consts<float>
   static __device__ __forceinline__ float P(const StageArgs &A, int d) { return A.Pf[d]; }
   static __device__ __forceinline__ float M(const StageArgs &A, int d) { return A.Mf[d]; }
   static __device__ __forceinline__ float skew(const StageArgs &A) { return A.skewf; }
+  static __device__ __forceinline__ float K1(const StageArgs &A, int d) { return A.K1f[d]; }
+  static __device__ __forceinline__ float K2(const StageArgs &A, int d) { return A.K2f[d]; }
+  static __device__ __forceinline__ float cdiff(const StageArgs &A, int d) { return A.cdifff[d]; }
+  static __device__ __forceinline__ float sa(const StageArgs &A) { return A.adv_scalef; }
 };
 
 template <int N, typename T>
@@ -143,11 +153,16 @@ __device__ __forceinline__ void sweep2(const T (&M)[kMaxNDev][kMaxNDev], const E
 // Face terms and volume term of one direction d for one pencil of Gauss-point
 // values U along d; returns the pencil's contribution to Z (without 1/det J).
 // Flo / Fhi: [P | M] coefficients of the low / high face (field case);
-// vt: det J (J^{-1} a)_d along the pencil (field case).
-template <int N, typename T, bool UNI, int D>
+// vt: det J (J^{-1} a)_d along the pencil (field case).  VISC adds the SIPG
+// terms of an affine mesh (advection_diffusion_solver.cc:531-613 in the
+// right-hand-side sign convention): dnlo / dnhi are the neighbour's reference
+// normal derivatives at the face points, blo / bhi mark Dirichlet faces
+// (mirror data u+ = 2g - u-, grad u+ = grad u-).
+template <int N, typename T, bool UNI, bool VISC, int D>
 __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTables<T> &tb,
-                                               const T (&U)[N], T nlo, T nhi, int fq, const T *Flo,
-                                               const T *Fhi, const T *vt, int vstride, T (&out)[N])
+                                               const T (&U)[N], T nlo, T nhi, T dnlo, T dnhi, bool blo,
+                                               bool bhi, int fq, const T *Flo, const T *Fhi, const T *vt,
+                                               int vstride, T (&out)[N])
 {
   constexpr int NF = N * N;
   T             ulo = tb.l0[0] * U[0], uhi = tb.l1[0] * U[0];
@@ -188,40 +203,82 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
       phlo       = fma(-sk * (Plo + Mlo), ulo, phlo);
       phhi       = fma(sk * (Phi + Mhi), uhi, phhi);
     }
-  // volume term: (1 - skew) (a u, grad v) - skew (a . grad u, v)
+  // with diffusion the velocity time factor is applied here (it does not
+  // scale the viscous terms); otherwise the caller folds it into b and a
+  const T sa = VISC ? Consts<T>::sa(A) : T(1);
+  if (VISC)
+    {
+      phlo *= sa;
+      phhi *= sa;
+    }
+  // volume term: (1 - skew) (a u, grad v) - skew (a . grad u, v) - nu (grad u, grad v)
   // (advection_solver.cc:500-507); with vt = det J J^{-1} a per Gauss point
-  T vtv[N], w[N];
+  T vtv[N], w[N], du[N];
+  const bool need_du = VISC || A.has_skew;
+  if (need_du)
+    sweep2<N, T, true>(tb.D, tb.D_eo, U, du);
+  const T sk  = A.has_skew ? Consts<T>::skew(A) : T(0);
+  const T adv = VISC ? (T(1) - sk) * sa : T(1) - sk;
 #pragma unroll
   for (int q = 0; q < N; ++q)
     {
       vtv[q] = UNI ? T(1) : vt[q * vstride];
       w[q]   = UNI ? U[q] : vtv[q] * U[q];
+      if (VISC)
+        w[q] = fma(adv, w[q], -Consts<T>::cdiff(A, D) * du[q]);
     }
   sweep2<N, T, true>(tb.Dw, tb.Dw_eo, w, out);
   if (A.has_skew)
     {
-      const T sk = Consts<T>::skew(A), oms = T(1) - sk;
-      T       du[N];
-      sweep2<N, T, true>(tb.D, tb.D_eo, U, du);
 #pragma unroll
       for (int q = 0; q < N; ++q)
-        out[q] = fma(oms, out[q], -sk * (UNI ? du[q] : vtv[q] * du[q]));
+        out[q] = VISC ? fma(-sk * sa, vtv[q] * du[q], out[q])
+                      : fma(T(1) - sk, out[q], -sk * (UNI ? du[q] : vtv[q] * du[q]));
+    }
+  // SIPG face terms: value coefficients join the flux, normal-derivative
+  // coefficients are lifted with l'(s) / w
+  T dlo = T(0), dhi = T(0);
+  if (VISC)
+    {
+      T duo_lo = tb.ld0[0] * U[0], duo_hi = tb.ld1[0] * U[0];
+#pragma unroll
+      for (int q = 1; q < N; ++q)
+        {
+          duo_lo = fma(tb.ld0[q], U[q], duo_lo);
+          duo_hi = fma(tb.ld1[q], U[q], duo_hi);
+        }
+      const T un_lo  = blo ? T(2) * nlo - ulo : nlo;
+      const T un_hi  = bhi ? T(2) * nhi - uhi : nhi;
+      const T dun_lo = blo ? duo_lo : dnlo;
+      const T dun_hi = bhi ? duo_hi : dnhi;
+      const T K1 = Consts<T>::K1(A, D), K2 = Consts<T>::K2(A, D);
+      const T jl = un_lo - ulo, jh = uhi - un_hi; // jumps u- - u+ across the low / high face
+      phlo       = fma(K1, jl, fma(-K2, dun_lo + duo_lo, phlo));
+      phhi       = fma(-K1, jh, fma(K2, duo_hi + dun_hi, phhi));
+      dlo        = K2 * jl;
+      dhi        = K2 * jh;
     }
   const T cv = Consts<T>::cv(A, D);
 #pragma unroll
   for (int q = 0; q < N; ++q)
     {
-      T o    = UNI ? cv * out[q] : out[q];
-      o      = fma(tb.lw0[q], phlo, o);
-      out[q] = fma(tb.lw1[q], phhi, o);
+      T o = UNI ? cv * out[q] : out[q];
+      o   = fma(tb.lw0[q], phlo, o);
+      o   = fma(tb.lw1[q], phhi, o);
+      if (VISC)
+        {
+          o = fma(tb.lwd0[q], dlo, o);
+          o = fma(tb.lwd1[q], dhi, o);
+        }
+      out[q] = o;
     }
 }
 
-template <int N, typename T, bool UNI>
-__global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
+template <int N, typename T, bool UNI, bool VISC>
+__global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS)
   stage_kernel(const StageArgs A)
 {
-  using SH         = StageShape<N, T, UNI>;
+  using SH         = StageShape<N, T, UNI, VISC>;
   constexpr int C  = SH::C;
   constexpr int NQ = SH::NQ;
   constexpr int NF = SH::NF;
@@ -232,7 +289,8 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
   T   *Nb     = Qb + C * NQ;                     // [C][6][NF] neighbour face values
   T   *Gb     = Nb + C * 6 * NF;                 // field: [C][4][NQ] cell geometry
   T   *Fb     = Gb + (UNI ? 0 : C * 4 * NQ);     // field: [C][6][2][NF] face coefficients
-  int *s_nbr  = reinterpret_cast<int *>(Fb + (UNI ? 0 : C * 12 * NF)); // [C][6] neighbour or -1
+  T   *Nd     = Fb + (UNI ? 0 : C * 12 * NF);    // viscous: [C][6][NF] neighbour normal derivatives
+  int *s_nbr  = reinterpret_cast<int *>(Nd + (VISC ? C * 6 * NF : 0)); // [C][6] neighbour or -1
   int *s_face = s_nbr + C * 6;                                          // [C][6] face id
 
   const DevTables<T> &tb    = tab<T>(N);
@@ -324,9 +382,41 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
         const int     stride = d == 0 ? N : 1;
         const double *g      = A.r_in + (long long)nb * NQ + base;
         T             in[N], out[N];
+        if (!VISC)
+          {
 #pragma unroll
-        for (int a = 0; a < N; ++a)
-          in[a] = from_double<T>(__ldg(g + a * stride));
+            for (int a = 0; a < N; ++a)
+              in[a] = from_double<T>(__ldg(g + a * stride));
+          }
+        else
+          {
+            // whole pencils through the neighbour along d: the face value and
+            // the reference normal derivative at the face (xi_d = 1 for the
+            // neighbour below, 0 for the one above)
+            const int     sd   = d == 0 ? 1 : d == 1 ? N : NF;
+            const double *g0   = g - layer * sd;
+            const T      *dphi = (j & 1) ? tb.dphi0 : tb.dphi1;
+            T             der[N], dout[N];
+#pragma unroll
+            for (int a = 0; a < N; ++a)
+              {
+                T v[N];
+#pragma unroll
+                for (int i = 0; i < N; ++i)
+                  v[i] = from_double<T>(__ldg(g0 + a * stride + i * sd));
+                in[a] = v[layer];
+                T dv  = dphi[0] * v[0];
+#pragma unroll
+                for (int i = 1; i < N; ++i)
+                  dv = fma(dphi[i], v[i], dv);
+                der[a] = dv;
+              }
+            sweep2<N, T, false>(tb.S, tb.S_eo, der, dout);
+            T *pd = Nd + cf * NF + N * b;
+#pragma unroll
+            for (int a = 0; a < N; ++a)
+              pd[a] = dout[a];
+          }
         sweep2<N, T, false>(tb.S, tb.S_eo, in, out);
         T *p = Nb + cf * NF + N * b;
 #pragma unroll
@@ -365,6 +455,17 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
 #pragma unroll
           for (int k = 0; k < N; ++k)
             p[k * N] = out[k];
+          if (VISC)
+            {
+              T *pd = Nd + cf * NF + q1;
+#pragma unroll
+              for (int k = 0; k < N; ++k)
+                in[k] = pd[k * N];
+              sweep2<N, T, false>(tb.S, tb.S_eo, in, out);
+#pragma unroll
+              for (int k = 0; k < N; ++k)
+                pd[k * N] = out[k];
+            }
         }
       else
         {
@@ -400,7 +501,10 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
       for (int k = 0; k < N; ++k)
         p[k] = U[k];
       const T *F = Fb + cl * 12 * NF;
-      direction_pass<N, T, UNI, 0>(A, tb, U, Nb[(cl * 6 + 0) * NF + r], Nb[(cl * 6 + 1) * NF + r], r,
+      direction_pass<N, T, UNI, VISC, 0>(A, tb, U, Nb[(cl * 6 + 0) * NF + r], Nb[(cl * 6 + 1) * NF + r],
+                                         VISC ? Nd[(cl * 6 + 0) * NF + r] : T(0),
+                                         VISC ? Nd[(cl * 6 + 1) * NF + r] : T(0),
+                                         s_nbr[cl * 6 + 0] < 0, s_nbr[cl * 6 + 1] < 0, r,
                                    F, F + 2 * NF, Gb + cl * 4 * NQ + N * r, 1, out);
       T *z = Qb + cl * NQ + N * r;
 #pragma unroll
@@ -420,7 +524,10 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
       for (int k = 0; k < N; ++k)
         U[k] = p[k * N];
       const T *F = Fb + cl * 12 * NF + 4 * NF;
-      direction_pass<N, T, UNI, 1>(A, tb, U, Nb[(cl * 6 + 2) * NF + r], Nb[(cl * 6 + 3) * NF + r], r,
+      direction_pass<N, T, UNI, VISC, 1>(A, tb, U, Nb[(cl * 6 + 2) * NF + r], Nb[(cl * 6 + 3) * NF + r],
+                                         VISC ? Nd[(cl * 6 + 2) * NF + r] : T(0),
+                                         VISC ? Nd[(cl * 6 + 3) * NF + r] : T(0),
+                                         s_nbr[cl * 6 + 2] < 0, s_nbr[cl * 6 + 3] < 0, r,
                                    F, F + 2 * NF, Gb + (cl * 4 + 1) * NQ + off, N, out);
       T *z = Qb + cl * NQ + off;
 #pragma unroll
@@ -440,7 +547,10 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
         U[k] = p[k * NF];
       const T *F = Fb + cl * 12 * NF + 8 * NF;
       const T *G = Gb + cl * 4 * NQ;
-      direction_pass<N, T, UNI, 2>(A, tb, U, Nb[(cl * 6 + 4) * NF + r], Nb[(cl * 6 + 5) * NF + r], r,
+      direction_pass<N, T, UNI, VISC, 2>(A, tb, U, Nb[(cl * 6 + 4) * NF + r], Nb[(cl * 6 + 5) * NF + r],
+                                         VISC ? Nd[(cl * 6 + 4) * NF + r] : T(0),
+                                         VISC ? Nd[(cl * 6 + 5) * NF + r] : T(0),
+                                         s_nbr[cl * 6 + 4] < 0, s_nbr[cl * 6 + 5] < 0, r,
                                    F, F + 2 * NF, G + 2 * NQ + r, NF, out);
       T *z = Qb + cl * NQ + r;
 #pragma unroll
@@ -513,10 +623,10 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI>::THREADS)
     }
 }
 
-template <int N, typename T, bool UNI>
+template <int N, typename T, bool UNI, bool VISC>
 cudaError_t launch_stage_t(const StageArgs &args, cudaStream_t stream)
 {
-  using SH = StageShape<N, T, UNI>;
+  using SH = StageShape<N, T, UNI, VISC>;
   // the shared-memory opt-in is a per-device function attribute
   static unsigned long long configured = 0;
   int                       dev        = 0;
@@ -525,21 +635,25 @@ cudaError_t launch_stage_t(const StageArgs &args, cudaStream_t stream)
     return e;
   if (dev >= 64 || !((configured >> dev) & 1ull))
     {
-      e = cudaFuncSetAttribute(stage_kernel<N, T, UNI>, cudaFuncAttributeMaxDynamicSharedMemorySize, SH::SMEM);
+      e = cudaFuncSetAttribute(stage_kernel<N, T, UNI, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               SH::SMEM);
       if (e != cudaSuccess)
         return e;
       if (dev < 64)
         configured |= 1ull << dev;
     }
   const long long blocks = (args.n_cells + SH::C - 1) / SH::C;
-  stage_kernel<N, T, UNI><<<(unsigned)blocks, SH::THREADS, SH::SMEM, stream>>>(args);
+  stage_kernel<N, T, UNI, VISC><<<(unsigned)blocks, SH::THREADS, SH::SMEM, stream>>>(args);
   return cudaGetLastError();
 }
 
 template <int N, typename T>
 cudaError_t launch_stage_n(const StageArgs &args, cudaStream_t stream)
 {
-  return args.uniform ? launch_stage_t<N, T, true>(args, stream) : launch_stage_t<N, T, false>(args, stream);
+  if (args.visc)
+    return launch_stage_t<N, T, false, true>(args, stream);
+  return args.uniform ? launch_stage_t<N, T, true, false>(args, stream)
+                      : launch_stage_t<N, T, false, false>(args, stream);
 }
 
 template <int N, typename T>

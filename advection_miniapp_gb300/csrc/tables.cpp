@@ -163,6 +163,10 @@ void Tables1D::init(int degree)
       l1[q]  = lagrange(gp, n, q, 1.0);
       lw0[q] = l0[q] / gw[q];
       lw1[q] = l1[q] / gw[q];
+      ld0[q]  = lagrange_derivative(gp, n, q, 0.0);
+      ld1[q]  = lagrange_derivative(gp, n, q, 1.0);
+      lwd0[q] = ld0[q] / gw[q];
+      lwd1[q] = ld1[q] / gw[q];
     }
   for (int i = 0; i < n; ++i)
     {

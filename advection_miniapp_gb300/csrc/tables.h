@@ -26,6 +26,8 @@ struct Tables1D
   double l0[kMaxN] = {}, l1[kMaxN] = {};   // l_q(0), l_q(1): Gauss-Lagrange basis at the faces
   double lw0[kMaxN] = {}, lw1[kMaxN] = {}; // l_q(s) / w_q
   double dphi0[kMaxN] = {}, dphi1[kMaxN] = {}; // phi_i'(0), phi_i'(1) of the nodal basis
+  double ld0[kMaxN] = {}, ld1[kMaxN] = {};     // l_q'(0), l_q'(1) of the Gauss-Lagrange basis
+  double lwd0[kMaxN] = {}, lwd1[kMaxN] = {};   // l_q'(s) / w_q
   double Sd[kMaxN][kMaxN] = {}; // Sd[q][i] = phi_i'(g_q)
 
   void init(int degree);

@@ -34,6 +34,13 @@ CASES = {
                         boundary_value=0),
     "box-domain": dict(degree=3, n_cells=(2, 3, 4), domain_lo=(-1.0, 0.0, 0.5), domain_hi=(1.0, 0.5, 2.0),
                        velocity=(0.3, -0.7, 0.2)),
+    # SIPG advection-diffusion (affine meshes)
+    "sipg-rotating-k3": dict(degree=3, n_cells=(3, 2, 2), periodic=0, velocity_type=1, velocity=(1.0, 1.0, 0.3),
+                             velocity_period=0.5, diffusion=1e-2, penalty_factor=1.0, initial_condition=1,
+                             ic_params=(0.3, 0.5, 0.5, 0.2), boundary_value=0),
+    "sipg-periodic-k2": dict(degree=2, n_cells=(3, 3, 3), diffusion=3e-2),
+    "sipg-exact-bc-k5-skew": dict(degree=5, n_cells=(2, 2, 3), periodic=0, diffusion=1e-3, factor_skew=0.5,
+                                  initial_condition=2, boundary_value=1),
 }
 
 
@@ -115,7 +122,7 @@ def test_perform_stage_aliasing_patterns(cuda, oracle_mod, adv_lib, case):
 
 
 @pytest.mark.parametrize("scheme", [0, 1, 2, 3])
-@pytest.mark.parametrize("case", ["affine-k3", "curved-k4", "rotating-k3"])
+@pytest.mark.parametrize("case", ["affine-k3", "curved-k4", "rotating-k3", "sipg-rotating-k3"])
 def test_lsrk_steps_match_oracle(cuda, oracle_mod, adv_lib, case, scheme):
     torch = cuda
     o, g = pair(oracle_mod, adv_lib, CASES[case])
@@ -248,3 +255,30 @@ def test_full_size_curved_properties(cuda, adv_lib):
         del g, u, r, k
         torch.cuda.empty_cache()
     assert rel_err(res[1], res[0]) <= 1e-5
+
+
+def test_advection_diffusion_workload_reduced(cuda, oracle_mod, adv_lib):
+    """The advection-diffusion workload (rotating field with T = 0.5, nu = 1e-3,
+    penalty (k+1)^2/h, Dirichlet-zero data, Gaussian blob of width 0.1 at
+    (0.3, 0.5, 0.5), degree 5) on 6^3 cells: 20 FP64 steps against the oracle,
+    and the FP32 operator close to FP64."""
+    torch = cuda
+    cfg = dict(degree=5, n_cells=(6, 6, 6), periodic=0, velocity_type=1, velocity=(1.0, 1.0, 0.3),
+               velocity_period=0.5, diffusion=1e-3, penalty_factor=1.0, initial_condition=1,
+               ic_params=(0.3, 0.5, 0.5, 0.1), boundary_value=0)
+    o = oracle_mod.Oracle(**cfg)
+    dt = o.time_step(0.5)
+    u = o.project(0.0)
+    r, k = o.zeros(), o.zeros()
+    for s in range(20):
+        o.lsrk_step(s * dt, dt, u, r, k)
+    res = {}
+    for precision in (0, 1):
+        g = adv_lib.AdvectionOperation(**cfg, precision=precision)
+        ud = g.initialize_dof_vector()
+        g.project_initial(ud)
+        rd, kd = g.initialize_dof_vector(), g.initialize_dof_vector()
+        g.lsrk_steps(adv_lib.LSRK_5_4, 0.0, dt, 20, ud, rd, kd)
+        res[precision] = ud.cpu().numpy()
+    assert rel_err(res[0], u) <= FP64_TOL
+    assert rel_err(res[1], u) <= 1e-5
