@@ -237,6 +237,7 @@ void fill_diag(adv_handle &h)
         g.S[q * n + i]  = h.tb.S[q][i];
         g.Sd[q * n + i] = h.tb.Sd[q][i];
         g.Si[q * n + i] = h.tb.Si[q][i];
+        g.Dc[q * n + i] = h.tb.D[q][i];
       }
   for (int p = 0; p < n + 1; ++p)
     for (int i = 0; i < n; ++i)

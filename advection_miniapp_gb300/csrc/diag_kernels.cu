@@ -2,9 +2,14 @@
 // (project_initial, advection_solver.cc:760-784), mass/energy/H1 seminorm
 // (compute_mass_and_energy, advection_solver.cc:787-818), the L2 error
 // against the analytic solution (output_results, advection_solver.cc:1183-1208)
-// and an FMA throughput probe for roofline denominators.  These run once per
-// output, not per stage; they favour simplicity (direct sums per point, one
-// CTA per cell) over speed.
+// and an FMA throughput probe for roofline denominators.
+//
+// FP64, one CTA per cell at a time (grid-stride), every evaluation by sum
+// factorization: 1D matrices applied direction by direction in shared memory,
+// one thread per output entry.  The curved mapping is evaluated from its
+// support points (the analytic deformation at the Gauss-Lobatto nodes), so
+// no geometry is stored for the diagnostics.  Reductions are deterministic:
+// per-CTA partials, summed by the caller.
 #include "kernels.h"
 
 namespace adv
@@ -12,7 +17,9 @@ namespace adv
 namespace
 {
 constexpr int kDiagThreads = 128;
-constexpr int kMaxNQ       = 343; // 7^3
+constexpr int kMaxP        = 8; // points per direction (error quadrature: n + 1 <= 8)
+constexpr int kMaxP3       = kMaxP * kMaxP * kMaxP;
+constexpr int kMaxN3       = 343;
 
 __device__ __forceinline__ void cell_origin(const DiagArgs &g, long long c, double lo[3])
 {
@@ -23,55 +30,81 @@ __device__ __forceinline__ void cell_origin(const DiagArgs &g, long long c, doub
   lo[2] = g.lo[2] + iz * g.h[2];
 }
 
-// support points of the curved mapping into X (3 per node)
-__device__ void load_support_points(const DiagArgs &g, const double lo[3], double *X)
+// out = A applied along direction d of `in` (dims d0 x d1 x d2, first fastest);
+// A is mo x ni row-major (A[q * ni + k]); the output has mo entries along d.
+// Ends with a barrier.
+__device__ void tsweep(const double *A, int mo, int ni, int d, int d0, int d1, int d2, const double *in,
+                       double *out)
+{
+  const int o0 = d == 0 ? mo : d0, o1 = d == 1 ? mo : d1, o2 = d == 2 ? mo : d2;
+  const int total = o0 * o1 * o2;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x)
+    {
+      const int i0 = idx % o0, i1 = (idx / o0) % o1, i2 = idx / (o0 * o1);
+      const int q  = d == 0 ? i0 : d == 1 ? i1 : i2;
+      const int st = d == 0 ? 1 : d == 1 ? d0 : d0 * d1;
+      const int b  = (d == 0 ? 0 : i0) + d0 * ((d == 1 ? 0 : i1) + d1 * (d == 2 ? 0 : i2));
+      double    s  = 0.0;
+      for (int k = 0; k < ni; ++k)
+        s += A[q * ni + k] * in[b + k * st];
+      out[idx] = s;
+    }
+  __syncthreads();
+}
+
+// support points of the curved mapping, component c, into X (n^3)
+__device__ void support_component(const DiagArgs &g, const double lo[3], int c, double *X)
 {
   const int n = g.n, nq = n * n * n;
   for (int i = threadIdx.x; i < nq; i += blockDim.x)
     {
-      const int    a = i % n, b = (i / n) % n, c = i / (n * n);
-      const double p[3] = {lo[0] + g.h[0] * g.gl[a], lo[1] + g.h[1] * g.gl[b], lo[2] + g.h[2] * g.gl[c]};
-      deform_dev(g.deformation, g.lo, g.L, p, X + 3 * i);
+      const int    a = i % n, b = (i / n) % n, cc = i / (n * n);
+      const double p[3] = {lo[0] + g.h[0] * g.gl[a], lo[1] + g.h[1] * g.gl[b], lo[2] + g.h[2] * g.gl[cc]};
+      double       y[3];
+      deform_dev(g.deformation, g.lo, g.L, p, y);
+      X[i] = y[c];
+    }
+  __syncthreads();
+}
+
+struct Scratch
+{
+  double *X, *A, *Az, *B, *By, *Bz;
+};
+
+// position x[c][p] and Jacobian J[3c + j][p] at the m^3 points of the 1D rule
+// with nodal-basis values V and derivatives W (m x n); curved cells only
+__device__ void map_points(const DiagArgs &g, const double lo[3], int m, const double *V, const double *W,
+                           double *x, double *J, const Scratch &s)
+{
+  const int n = g.n, m3 = m * m * m;
+  for (int c = 0; c < 3; ++c)
+    {
+      support_component(g, lo, c, s.X);
+      tsweep(V, m, n, 2, n, n, n, s.X, s.A);
+      tsweep(W, m, n, 2, n, n, n, s.X, s.Az);
+      tsweep(V, m, n, 1, n, n, m, s.A, s.B);
+      tsweep(W, m, n, 1, n, n, m, s.A, s.By);
+      tsweep(V, m, n, 1, n, n, m, s.Az, s.Bz);
+      tsweep(V, m, n, 0, n, m, m, s.B, x + c * m3);
+      tsweep(W, m, n, 0, n, m, m, s.B, J + (3 * c + 0) * m3);
+      tsweep(V, m, n, 0, n, m, m, s.By, J + (3 * c + 1) * m3);
+      tsweep(V, m, n, 0, n, m, m, s.Bz, J + (3 * c + 2) * m3);
     }
 }
 
-// position and Jacobian at a reference point given 1D basis values V[d][a]
-// and derivatives W[d][a] (curved: sums over the support points)
-__device__ void map_at(const DiagArgs &g, const double lo[3], const double *X, const double *V0,
-                       const double *V1, const double *V2, const double *W0, const double *W1,
-                       const double *W2, const double xi[3], double x[3], double J[9])
+// J at point p from the component arrays, or the affine Jacobian
+__device__ void jacobian_at(const DiagArgs &g, const double *J, int m3, int p, double Jp[9])
 {
-  const int n = g.n;
   if (!g.curved)
     {
-      for (int d = 0; d < 3; ++d)
-        x[d] = lo[d] + g.h[d] * xi[d];
       for (int i = 0; i < 9; ++i)
-        J[i] = 0.0;
-      J[0] = g.h[0], J[4] = g.h[1], J[8] = g.h[2];
+        Jp[i] = 0.0;
+      Jp[0] = g.h[0], Jp[4] = g.h[1], Jp[8] = g.h[2];
       return;
     }
-  for (int d = 0; d < 3; ++d)
-    x[d] = 0.0;
   for (int i = 0; i < 9; ++i)
-    J[i] = 0.0;
-  for (int c = 0; c < n; ++c)
-    for (int b = 0; b < n; ++b)
-      for (int a = 0; a < n; ++a)
-        {
-          const double *y  = X + 3 * (a + n * (b + n * c));
-          const double  w  = V0[a] * V1[b] * V2[c];
-          const double  w0 = W0[a] * V1[b] * V2[c];
-          const double  w1 = V0[a] * W1[b] * V2[c];
-          const double  w2 = V0[a] * V1[b] * W2[c];
-          for (int d = 0; d < 3; ++d)
-            {
-              x[d] += w * y[d];
-              J[3 * d + 0] += w0 * y[d];
-              J[3 * d + 1] += w1 * y[d];
-              J[3 * d + 2] += w2 * y[d];
-            }
-        }
+    Jp[i] = J[i * m3 + p];
 }
 
 __device__ double det_inv3(const double *J, double *Ji)
@@ -91,26 +124,19 @@ __device__ double det_inv3(const double *J, double *Ji)
   return det;
 }
 
-// in-place 1D sweep along direction d of an n^3 shared array with matrix M[q*n+i]
-__device__ void sweep_smem(int n, const double *M, double *a, int d)
+__device__ void point_position(const DiagArgs &g, const double lo[3], const double *pts, int m, int p,
+                               const double *x, double xp[3])
 {
-  const int stride = d == 0 ? 1 : d == 1 ? n : n * n;
-  for (int w = threadIdx.x; w < n * n; w += blockDim.x)
+  if (g.curved)
     {
-      const int r    = w % n, s = w / n;
-      const int base = d == 0 ? n * (r + n * s) : d == 1 ? r + n * n * s : r + n * s;
-      double    in[kMaxNDev];
-      for (int i = 0; i < n; ++i)
-        in[i] = a[base + i * stride];
-      for (int q = 0; q < n; ++q)
-        {
-          double s2 = 0.0;
-          for (int i = 0; i < n; ++i)
-            s2 += M[q * n + i] * in[i];
-          a[base + q * stride] = s2;
-        }
+      const int m3 = m * m * m;
+      xp[0] = x[p], xp[1] = x[m3 + p], xp[2] = x[2 * m3 + p];
+      return;
     }
-  __syncthreads();
+  const int i0 = p % m, i1 = (p / m) % m, i2 = p / (m * m);
+  xp[0] = lo[0] + g.h[0] * pts[i0];
+  xp[1] = lo[1] + g.h[1] * pts[i1];
+  xp[2] = lo[2] + g.h[2] * pts[i2];
 }
 
 __device__ void block_reduce3(double v0, double v1, double v2, double *out)
@@ -135,149 +161,150 @@ __device__ void block_reduce3(double v0, double v1, double v2, double *out)
     }
 }
 
+// shared-memory layout (doubles): X, A, Az, B, By, Bz, x[3], J[9], U, T1, T2, T3
+constexpr int kSmemDoubles = kMaxN3 + 2 * kMaxP * kMaxP * 7 + 3 * kMaxP * kMaxP * 7 + 12 * kMaxP3 + kMaxN3 +
+                             3 * kMaxP3;
+
+struct Layout
+{
+  Scratch s;
+  double *x, *J, *U, *T1, *T2, *T3;
+  __device__ explicit Layout(double *base)
+  {
+    s.X  = base;
+    s.A  = s.X + kMaxN3;
+    s.Az = s.A + kMaxP * kMaxP * 7;
+    s.B  = s.Az + kMaxP * kMaxP * 7;
+    s.By = s.B + kMaxP * kMaxP * 7;
+    s.Bz = s.By + kMaxP * kMaxP * 7;
+    x    = s.Bz + kMaxP * kMaxP * 7;
+    J    = x + 3 * kMaxP3;
+    U    = J + 9 * kMaxP3;
+    T1   = U + kMaxN3;
+    T2   = T1 + kMaxP3;
+    T3   = T2 + kMaxP3;
+  }
+};
+
 __global__ void __launch_bounds__(kDiagThreads) project_kernel(const DiagArgs g, double t, double *dst)
 {
-  __shared__ double X[3 * kMaxNQ];
-  __shared__ double V[kMaxNQ];
-  __shared__ double S[kMaxNDev * kMaxNDev], Si[kMaxNDev * kMaxNDev];
+  extern __shared__ __align__(16) double smem[];
+  Layout    L(smem);
   const int n = g.n, nq = n * n * n;
-  for (int i = threadIdx.x; i < n * n; i += blockDim.x)
-    S[i] = g.S[i], Si[i] = g.Si[i];
   for (long long c = blockIdx.x; c < g.n_cells; c += gridDim.x)
     {
       double lo[3];
       cell_origin(g, c, lo);
-      __syncthreads();
       if (g.curved)
-        load_support_points(g, lo, X);
-      __syncthreads();
+        map_points(g, lo, n, g.S, g.Sd, L.x, L.J, L.s);
       for (int q = threadIdx.x; q < nq; q += blockDim.x)
         {
-          const int    q0 = q % n, q1 = (q / n) % n, q2 = q / (n * n);
-          const double xi[3] = {g.gp[q0], g.gp[q1], g.gp[q2]};
-          double       x[3], J[9];
-          map_at(g, lo, X, S + q0 * n, S + q1 * n, S + q2 * n, S, S, S, xi, x, J);
-          V[q] = exact_value(g.ex, x[0], x[1], x[2], t);
+          double xp[3];
+          point_position(g, lo, g.gp, n, q, L.x, xp);
+          L.T1[q] = exact_value(g.ex, xp[0], xp[1], xp[2], t);
         }
       __syncthreads();
-      sweep_smem(n, Si, V, 0);
-      sweep_smem(n, Si, V, 1);
-      sweep_smem(n, Si, V, 2);
+      // transform_from_q_points_to_basis: S^{-1} in every direction
+      tsweep(g.Si, n, n, 0, n, n, n, L.T1, L.T2);
+      tsweep(g.Si, n, n, 1, n, n, n, L.T2, L.T3);
+      tsweep(g.Si, n, n, 2, n, n, n, L.T3, L.T1);
       for (int i = threadIdx.x; i < nq; i += blockDim.x)
-        dst[c * nq + i] = V[i];
+        dst[c * nq + i] = L.T1[i];
+      __syncthreads();
     }
 }
 
 __global__ void __launch_bounds__(kDiagThreads)
   mass_energy_kernel(const DiagArgs g, const double *u, double *partials)
 {
-  __shared__ double X[3 * kMaxNQ];
-  __shared__ double U[kMaxNQ];
-  __shared__ double S[kMaxNDev * kMaxNDev], Sd[kMaxNDev * kMaxNDev];
+  extern __shared__ __align__(16) double smem[];
+  Layout    L(smem);
   const int n = g.n, nq = n * n * n;
-  for (int i = threadIdx.x; i < n * n; i += blockDim.x)
-    S[i] = g.S[i], Sd[i] = g.Sd[i];
-  double m = 0.0, e = 0.0, hs = 0.0;
+  double    m = 0.0, e = 0.0, hs = 0.0;
+  double   *G[3] = {L.s.A, L.s.B, L.s.By}; // reuse scratch for the three gradients
   for (long long c = blockIdx.x; c < g.n_cells; c += gridDim.x)
     {
       double lo[3];
       cell_origin(g, c, lo);
-      __syncthreads();
       if (g.curved)
-        load_support_points(g, lo, X);
+        map_points(g, lo, n, g.S, g.Sd, L.x, L.J, L.s);
       for (int i = threadIdx.x; i < nq; i += blockDim.x)
-        U[i] = u[c * nq + i];
+        L.U[i] = u[c * nq + i];
       __syncthreads();
+      tsweep(g.S, n, n, 0, n, n, n, L.U, L.T1);
+      tsweep(g.S, n, n, 1, n, n, n, L.T1, L.T2);
+      tsweep(g.S, n, n, 2, n, n, n, L.T2, L.T3); // values at the Gauss points
+      for (int d = 0; d < 3; ++d)
+        tsweep(g.Dc, n, n, d, n, n, n, L.T3, G[d]);
       for (int q = threadIdx.x; q < nq; q += blockDim.x)
         {
+          double Jp[9], Ji[9];
+          jacobian_at(g, L.J, nq, q, Jp);
+          const double det = det_inv3(Jp, Ji);
           const int    q0 = q % n, q1 = (q / n) % n, q2 = q / (n * n);
-          const double xi[3] = {g.gp[q0], g.gp[q1], g.gp[q2]};
-          double       x[3], J[9], Ji[9];
-          map_at(g, lo, X, S + q0 * n, S + q1 * n, S + q2 * n, Sd + q0 * n, Sd + q1 * n,
-                 Sd + q2 * n, xi, x, J);
-          const double det = det_inv3(J, Ji);
-          double       v = 0.0, g0 = 0.0, g1 = 0.0, g2 = 0.0;
-          for (int cc = 0; cc < n; ++cc)
-            for (int b = 0; b < n; ++b)
-              for (int a = 0; a < n; ++a)
-                {
-                  const double ua = U[a + n * (b + n * cc)];
-                  v += S[q0 * n + a] * S[q1 * n + b] * S[q2 * n + cc] * ua;
-                  g0 += Sd[q0 * n + a] * S[q1 * n + b] * S[q2 * n + cc] * ua;
-                  g1 += S[q0 * n + a] * Sd[q1 * n + b] * S[q2 * n + cc] * ua;
-                  g2 += S[q0 * n + a] * S[q1 * n + b] * Sd[q2 * n + cc] * ua;
-                }
           const double JxW = det * g.gw[q0] * g.gw[q1] * g.gw[q2];
+          const double v   = L.T3[q];
           double       gg  = 0.0;
           for (int i = 0; i < 3; ++i)
             {
-              const double gi = Ji[0 * 3 + i] * g0 + Ji[1 * 3 + i] * g1 + Ji[2 * 3 + i] * g2;
+              const double gi = Ji[0 * 3 + i] * G[0][q] + Ji[1 * 3 + i] * G[1][q] + Ji[2 * 3 + i] * G[2][q];
               gg += gi * gi;
             }
           m += v * JxW;
           e += v * v * JxW;
           hs += gg * JxW;
         }
+      __syncthreads();
     }
-  __syncthreads();
   block_reduce3(m, e, hs, partials + 3 * blockIdx.x);
 }
 
 __global__ void __launch_bounds__(kDiagThreads)
   l2_error_kernel(const DiagArgs g, const double *u, double t, double *partials)
 {
-  __shared__ double X[3 * kMaxNQ];
-  __shared__ double U[kMaxNQ];
-  __shared__ double S[kMaxNDev * kMaxNDev], Sd[kMaxNDev * kMaxNDev];
-  __shared__ double SE[8 * kMaxNDev], SEd[8 * kMaxNDev];
-  const int n = g.n, nq = n * n * n, m = n + 1, meq = m * m * m;
-  for (int i = threadIdx.x; i < n * n; i += blockDim.x)
-    S[i] = g.S[i], Sd[i] = g.Sd[i];
-  for (int i = threadIdx.x; i < m * n; i += blockDim.x)
-    SE[i] = g.SE[i], SEd[i] = g.SEd[i];
-  double err = 0.0, nrm = 0.0;
+  extern __shared__ __align__(16) double smem[];
+  Layout    L(smem);
+  const int n = g.n, nq = n * n * n, m = n + 1, m3 = m * m * m;
+  double    err = 0.0, nrm = 0.0;
   for (long long c = blockIdx.x; c < g.n_cells; c += gridDim.x)
     {
       double lo[3];
       cell_origin(g, c, lo);
-      __syncthreads();
-      if (g.curved)
-        load_support_points(g, lo, X);
       for (int i = threadIdx.x; i < nq; i += blockDim.x)
-        U[i] = u[c * nq + i];
+        L.U[i] = u[c * nq + i];
       __syncthreads();
-      for (int p = threadIdx.x; p < meq; p += blockDim.x)
+      // u_h at the QGauss(k+2) points
+      tsweep(g.SE, m, n, 0, n, n, n, L.U, L.T1);
+      tsweep(g.SE, m, n, 1, m, n, n, L.T1, L.T2);
+      tsweep(g.SE, m, n, 2, m, m, n, L.T2, L.T3);
+      if (g.curved)
+        map_points(g, lo, m, g.SE, g.SEd, L.x, L.J, L.s);
+      for (int p = threadIdx.x; p < m3; p += blockDim.x)
         {
+          double xp[3], Jp[9], Ji[9];
+          point_position(g, lo, g.ep, m, p, L.x, xp);
+          jacobian_at(g, L.J, m3, p, Jp);
+          const double det = det_inv3(Jp, Ji);
           const int    p0 = p % m, p1 = (p / m) % m, p2 = p / (m * m);
-          const double xi[3] = {g.ep[p0], g.ep[p1], g.ep[p2]};
-          double       x[3], J[9], Ji[9];
-          map_at(g, lo, X, SE + p0 * n, SE + p1 * n, SE + p2 * n, SEd + p0 * n, SEd + p1 * n,
-                 SEd + p2 * n, xi, x, J);
-          const double det = det_inv3(J, Ji);
-          double       uh  = 0.0;
-          for (int cc = 0; cc < n; ++cc)
-            for (int b = 0; b < n; ++b)
-              {
-                const double w = SE[p1 * n + b] * SE[p2 * n + cc];
-                for (int a = 0; a < n; ++a)
-                  uh += w * SE[p0 * n + a] * U[a + n * (b + n * cc)];
-              }
-          const double d = uh - exact_value(g.ex, x[0], x[1], x[2], t);
+          const double d   = L.T3[p] - exact_value(g.ex, xp[0], xp[1], xp[2], t);
           err += d * d * det * g.ew[p0] * g.ew[p1] * g.ew[p2];
         }
+      __syncthreads();
+      // norm of the exact solution with QGauss(k+1)
+      if (g.curved)
+        map_points(g, lo, n, g.S, g.Sd, L.x, L.J, L.s);
       for (int q = threadIdx.x; q < nq; q += blockDim.x)
         {
+          double xp[3], Jp[9], Ji[9];
+          point_position(g, lo, g.gp, n, q, L.x, xp);
+          jacobian_at(g, L.J, nq, q, Jp);
+          const double det = det_inv3(Jp, Ji);
           const int    q0 = q % n, q1 = (q / n) % n, q2 = q / (n * n);
-          const double xi[3] = {g.gp[q0], g.gp[q1], g.gp[q2]};
-          double       x[3], J[9], Ji[9];
-          map_at(g, lo, X, S + q0 * n, S + q1 * n, S + q2 * n, Sd + q0 * n, Sd + q1 * n,
-                 Sd + q2 * n, xi, x, J);
-          const double det = det_inv3(J, Ji);
-          const double ue  = exact_value(g.ex, x[0], x[1], x[2], t);
+          const double ue  = exact_value(g.ex, xp[0], xp[1], xp[2], t);
           nrm += ue * ue * det * g.gw[q0] * g.gw[q1] * g.gw[q2];
         }
+      __syncthreads();
     }
-  __syncthreads();
   block_reduce3(err, nrm, 0.0, partials + 3 * blockIdx.x);
 }
 
@@ -293,6 +320,27 @@ __global__ void fma_peak_kernel(T *out, int iters, T a, T b)
     }
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
+
+constexpr size_t kSmemBytes = kSmemDoubles * sizeof(double);
+
+template <typename K>
+cudaError_t opt_in(K kernel)
+{
+  static unsigned long long configured = 0;
+  int                       dev        = 0;
+  cudaError_t               e          = cudaGetDevice(&dev);
+  if (e != cudaSuccess)
+    return e;
+  if (dev >= 64 || !((configured >> dev) & 1ull))
+    {
+      e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+      if (e != cudaSuccess)
+        return e;
+      if (dev < 64)
+        configured |= 1ull << dev;
+    }
+  return cudaSuccess;
+}
 } // namespace
 
 cudaError_t upload_tables_diag(const DevTables<double> *d, const DevTables<float> *f)
@@ -307,23 +355,29 @@ int diag_max_blocks(long long n_cells)
 
 cudaError_t launch_project(const DiagArgs &g, double t, double *dst, cudaStream_t s)
 {
-  project_kernel<<<diag_max_blocks(g.n_cells), kDiagThreads, 0, s>>>(g, t, dst);
+  if (cudaError_t e = opt_in(project_kernel))
+    return e;
+  project_kernel<<<diag_max_blocks(g.n_cells), kDiagThreads, kSmemBytes, s>>>(g, t, dst);
   return cudaGetLastError();
 }
 
 cudaError_t launch_mass_energy(const DiagArgs &g, const double *u, double *partials, int *n_blocks,
                                cudaStream_t s)
 {
+  if (cudaError_t e = opt_in(mass_energy_kernel))
+    return e;
   *n_blocks = diag_max_blocks(g.n_cells);
-  mass_energy_kernel<<<*n_blocks, kDiagThreads, 0, s>>>(g, u, partials);
+  mass_energy_kernel<<<*n_blocks, kDiagThreads, kSmemBytes, s>>>(g, u, partials);
   return cudaGetLastError();
 }
 
 cudaError_t launch_l2_error(const DiagArgs &g, const double *u, double t, double *partials,
                             int *n_blocks, cudaStream_t s)
 {
+  if (cudaError_t e = opt_in(l2_error_kernel))
+    return e;
   *n_blocks = diag_max_blocks(g.n_cells);
-  l2_error_kernel<<<*n_blocks, kDiagThreads, 0, s>>>(g, u, t, partials);
+  l2_error_kernel<<<*n_blocks, kDiagThreads, kSmemBytes, s>>>(g, u, t, partials);
   return cudaGetLastError();
 }
 

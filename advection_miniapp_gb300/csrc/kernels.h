@@ -87,6 +87,7 @@ struct DiagArgs
   double gl[8], gp[8], gw[8], ep[8], ew[8];
   double S[49], Si[49], Sd[49];
   double SE[56], SEd[56];
+  double Dc[49]; // collocation derivative on the Gauss points [q * n + p]
 };
 cudaError_t launch_project(const DiagArgs &g, double t, double *dst, cudaStream_t s);
 // partial sums per block written to `partials` (3 per block); returns number of blocks
