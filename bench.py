@@ -350,7 +350,11 @@ def ours(args):
     inst = (4 * fp_work_per_cell(n)[0] + fp_work_per_cell(n, stage=False)[0]) / STAGES
     flops = (4 * fp_work_per_cell(n)[1] + fp_work_per_cell(n, stage=False)[1]) / STAGES
     vec_bytes_launch = bytes_per_dof_step() / STAGES * n_dofs
-    achieved64 = flops * n_cells / launch64 / 1e12
+    # FP64 instructions of any kind (FMA, add, mul) take one issue slot of the
+    # FP64 pipe; expressed as FMA-equivalent TFLOP/s (2 flops per slot) they
+    # compare with the measured FMA peak
+    achieved64 = 2 * inst * n_cells / launch64 / 1e12
+    algorithmic64 = flops * n_cells / launch64 / 1e12
     achieved32_hbm = vec_bytes_launch / launch32 / 1e9
     geo32 = geometry_bytes_per_dof(n, 4) * n_dofs / launch32 / 1e9
     geo64 = geometry_bytes_per_dof(n, 8) * n_dofs / launch64 / 1e9
@@ -386,6 +390,9 @@ def ours(args):
         "roofline": {"bound": "fp64", "achieved": round(achieved64, 4), "peak": round(fp64_peak, 4),
                      "unit": "TFLOP/s", "frac": round(achieved64 / fp64_peak, 4), "traffic": None,
                      "peak_source": "FP64 FMA microbenchmark (adv_measure_fma_peak) on this GPU",
+                     "achieved_definition": "2 x FP64 instructions per second (each FP64 add/mul/FMA takes one "
+                                            "FMA issue slot); algorithmic_tflops counts FMA = 2, add/mul = 1",
+                     "algorithmic_tflops": round(algorithmic64, 4),
                      "flops_per_cell": flops, "fp64_inst_per_cell": inst,
                      "fp64_inst_frac": round(inst * n_cells / launch64 / (fp64_peak * 1e12 / 2), 4),
                      "hbm_achieved_gbs": round(vec_bytes_launch / launch64 / 1e9 + geo64, 2),
