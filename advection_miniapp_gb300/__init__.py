@@ -16,7 +16,7 @@ from ._lib import (AdvConfig, AdvError, BOUNDARY_EXACT, BOUNDARY_ZERO, IC_BLOB, 
                    PRECISION_FP32_OPERATOR, PRECISION_FP64, VELOCITY_CONSTANT, VELOCITY_ROTATING)
 
 __all__ = [
-    "AdvConfig", "AdvError", "AdvectionOperation", "LowStorageRungeKuttaIntegrator", "make_config",
+    "AdvConfig", "AdvError", "AdvectionOperation", "ImplicitSolver", "LowStorageRungeKuttaIntegrator", "make_config",
     "workload_config", "lsrk_coefficients", "measure_fma_peak",
 ]
 
@@ -45,6 +45,12 @@ def workload_config(name, precision=PRECISION_FP64, **overrides):
       velocity (1, 0.15, -0.05), sine-product + Gaussian initial data, upwind.
     * ``"deformed-k4-64"``: the same PDE on 64^3 cells of the sine-deformed
       cube (amplitude 0.08), degree 4, 32,768,000 DoFs.
+    * ``"deformed-k4-32"``: 32^3 deformed cells, degree 4, 4,096,000 DoFs (the
+      implicit BDF2 workload).
+    * ``"advection-diffusion-k5-32"``: 32^3 affine cells, degree 5, rotating
+      field times cos(pi t / 0.5), SIPG diffusion 1e-3 with penalty
+      (k+1)^2/h, Dirichlet-zero boundaries, Gaussian blob of width 0.1 at
+      (0.3, 0.5, 0.5).
     """
     base = dict(velocity=(1.0, 0.15, -0.05), flux_alpha=1.0, initial_condition=IC_SINE_GAUSS,
                 periodic=1, precision=precision)
@@ -52,6 +58,13 @@ def workload_config(name, precision=PRECISION_FP64, **overrides):
         base.update(degree=3, n_cells=(8, 8, 8), mesh_type=MESH_CARTESIAN)
     elif name == "deformed-k4-64":
         base.update(degree=4, n_cells=(64, 64, 64), mesh_type=MESH_DEFORMED, deformation=0.08)
+    elif name == "deformed-k4-32":
+        base.update(degree=4, n_cells=(32, 32, 32), mesh_type=MESH_DEFORMED, deformation=0.08)
+    elif name == "advection-diffusion-k5-32":
+        base.update(degree=5, n_cells=(32, 32, 32), mesh_type=MESH_CARTESIAN, periodic=0,
+                    velocity_type=VELOCITY_ROTATING, velocity=(1.0, 1.0, 0.3), velocity_period=0.5,
+                    diffusion=1e-3, penalty_factor=1.0, initial_condition=IC_BLOB,
+                    ic_params=(0.3, 0.5, 0.5, 0.1), boundary_value=BOUNDARY_ZERO)
     else:
         raise KeyError(name)
     base.update(overrides)
@@ -175,6 +188,16 @@ class AdvectionOperation:
         _lib.check(self._lib.adv_device_bytes(self._h, ctypes.byref(n)), "adv_device_bytes")
         return n.value
 
+    # -- implicit operator (advection_solver_implicit.cc) ---------------------
+    def vmult(self, src, dst, mass_factor, time=0.0, stream=None):
+        """dst = mass_factor M src - L(t) src (the reference's vmult = M/dt + A)."""
+        _lib.check(self._lib.adv_vmult(self._h, self._ptr(src), self._ptr(dst), float(mass_factor), float(time),
+                                       _stream_handle(stream)), "adv_vmult")
+
+    def apply_mass(self, src, dst, stream=None):
+        _lib.check(self._lib.adv_apply_mass(self._h, self._ptr(src), self._ptr(dst), _stream_handle(stream)),
+                   "adv_apply_mass")
+
     # -- fused time stepping -------------------------------------------------
     def lsrk_steps(self, scheme, time, time_step, n_steps, solution, vec_ri, vec_ki, stream=None):
         _lib.check(self._lib.adv_lsrk_steps(
@@ -211,3 +234,52 @@ class LowStorageRungeKuttaIntegrator:
                                        0.0 if stage == len(bi) - 1 else ai[stage] * time_step,
                                        vec_ri, vec_ki, solution, vec_ri)
             sum_previous_bi += bi[stage - 1]
+
+
+class ImplicitSolver:
+    """FGMRES(restart) with the block-Jacobi FDM preconditioner and BDF2 steps
+    (the implicit path of advection_solver_implicit.cc on the GPU)."""
+
+    def __init__(self, op, restart=30, precond_precision=PRECISION_FP32_OPERATOR):
+        self.op = op
+        self._lib = op._lib
+        self._s = ctypes.c_void_p()
+        _lib.check(self._lib.adv_solver_create(op._h, int(restart), int(precond_precision), ctypes.byref(self._s)),
+                   "adv_solver_create")
+
+    def close(self):
+        if getattr(self, "_s", None):
+            self._lib.adv_solver_destroy(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def device_bytes(self):
+        n = ctypes.c_int64()
+        _lib.check(self._lib.adv_solver_device_bytes(self._s, ctypes.byref(n)), "adv_solver_device_bytes")
+        return n.value
+
+    def precondition(self, src, dst, mass_factor, time=0.0, stream=None):
+        _lib.check(self._lib.adv_precondition(self._s, self.op._ptr(src), self.op._ptr(dst), float(mass_factor),
+                                              float(time), _stream_handle(stream)), "adv_precondition")
+
+    def fgmres(self, mass_factor, time, rhs, x, rel_tol=1e-10, max_iterations=1000, stream=None):
+        """Solve (mass_factor M - L) x = rhs from the initial guess in x; returns (iterations, relative residual)."""
+        its, res = ctypes.c_int(), ctypes.c_double()
+        _lib.check(self._lib.adv_fgmres(self._s, float(mass_factor), float(time), self.op._ptr(rhs), self.op._ptr(x),
+                                        float(rel_tol), int(max_iterations), ctypes.byref(its), ctypes.byref(res),
+                                        _stream_handle(stream)), "adv_fgmres")
+        return its.value, res.value
+
+    def bdf2_step(self, t_new, dt, first_step, u_n, u_nm1, u_new, rel_tol=1e-10, stream=None):
+        """One BDF2 step (implicit Euler when first_step); returns the FGMRES iterations."""
+        its = ctypes.c_int()
+        _lib.check(self._lib.adv_bdf2_step(self._s, float(t_new), float(dt), int(bool(first_step)),
+                                           self.op._ptr(u_n), self.op._ptr(u_nm1) if u_nm1 is not None else None,
+                                           self.op._ptr(u_new), float(rel_tol), ctypes.byref(its),
+                                           _stream_handle(stream)), "adv_bdf2_step")
+        return its.value

@@ -74,6 +74,15 @@ SIGNATURES = {
     "adv_launch_count": (_I, [_P, ctypes.POINTER(_I64)]),
     "adv_measure_fma_peak": (_I, [_I, _DP, _P]),
     "adv_perform_stage_noalloc": (_I, [_P, _D, _D, _D, _P, _P, _P, _P, _P]),
+    "adv_fdm_tables": (_I, [_I, _D, _I, _DP, _DP, _DP, _DP, _DP]),
+    "adv_vmult": (_I, [_P, _P, _P, _D, _D, _P]),
+    "adv_apply_mass": (_I, [_P, _P, _P, _P]),
+    "adv_solver_create": (_I, [_P, _I, _I, ctypes.POINTER(_P)]),
+    "adv_solver_destroy": (_I, [_P]),
+    "adv_solver_device_bytes": (_I, [_P, ctypes.POINTER(_I64)]),
+    "adv_precondition": (_I, [_P, _P, _P, _D, _D, _P]),
+    "adv_fgmres": (_I, [_P, _D, _D, _P, _P, _D, _I, ctypes.POINTER(_I), _DP, _P]),
+    "adv_bdf2_step": (_I, [_P, _D, _D, _I, _P, _P, _P, _D, ctypes.POINTER(_I), _P]),
 }
 
 _lib = None

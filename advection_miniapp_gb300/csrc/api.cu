@@ -15,34 +15,22 @@
 #include <vector>
 
 #include "../../include/advection_gb300.h"
+#include "fdm.h"
 #include "geometry.h"
+#include "handle.h"
+#include "implicit_kernels.h"
 #include "kernels.h"
 #include "tables.h"
-
-struct adv_handle
-{
-  adv_config       cfg;
-  adv::Mesh        mesh;
-  adv::Tables1D    tb;
-  int              device = 0;
-  double           h_min  = 0.0;
-  // uniform-case constants
-  double cv[3] = {}, P[3] = {}, M[3] = {};
-  // device buffers
-  void    *d_cell_geo    = nullptr;
-  void    *d_face_geo[3] = {};
-  double  *d_face_x[3]   = {};
-  double  *d_partials    = nullptr;
-  double  *d_scratch[2]  = {};
-  int64_t  device_bytes  = 0;
-  int64_t  launches      = 0;
-  adv::DiagArgs diag;
-};
 
 namespace
 {
 thread_local std::string g_last_error;
+} // namespace
 
+namespace adv
+{
+namespace detail
+{
 int fail(int code, const std::string &msg)
 {
   g_last_error = msg;
@@ -54,15 +42,14 @@ int cuda_fail(cudaError_t e, const char *where)
   g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
   return e == cudaErrorMemoryAllocation ? ADV_ERR_OUT_OF_MEMORY : ADV_ERR_CUDA;
 }
+} // namespace detail
+} // namespace adv
 
-#define ADV_CUDA(call)                               \
-  do                                                 \
-    {                                                \
-      cudaError_t e_ = (call);                       \
-      if (e_ != cudaSuccess)                         \
-        return cuda_fail(e_, #call);                 \
-    }                                                \
-  while (0)
+using adv::detail::cuda_fail;
+using adv::detail::fail;
+
+namespace
+{
 
 std::mutex g_table_mutex;
 bool       g_tables_uploaded[256] = {};
@@ -133,6 +120,21 @@ int ensure_tables(int device)
       for (int i = 0; i < n; ++i)
         for (int q = 0; q < n; ++q)
           Si[i][q] = t.Si[i][q];
+      double St[adv::kMaxN][adv::kMaxN] = {}, SiT[adv::kMaxN][adv::kMaxN] = {};
+      for (int i = 0; i < n; ++i)
+        for (int q = 0; q < n; ++q)
+          {
+            St[i][q]        = t.S[q][i];
+            SiT[q][i]       = t.Si[i][q];
+            td[n].St[i][q]  = t.S[q][i];
+            td[n].SiT[q][i] = t.Si[i][q];
+            tf[n].St[i][q]  = (float)t.S[q][i];
+            tf[n].SiT[q][i] = (float)t.Si[i][q];
+          }
+      even_odd(n, St, false, td[n].St_eo);
+      even_odd(n, SiT, false, td[n].SiT_eo);
+      even_odd(n, St, false, tf[n].St_eo);
+      even_odd(n, SiT, false, tf[n].SiT_eo);
       even_odd(n, t.S, false, td[n].S_eo);
       even_odd(n, Si, false, td[n].Si_eo);
       even_odd(n, t.Dw, true, td[n].Dw_eo);
@@ -145,6 +147,7 @@ int ensure_tables(int device)
   ADV_CUDA(adv::upload_tables_stage64(td, tf));
   ADV_CUDA(adv::upload_tables_stage32(td, tf));
   ADV_CUDA(adv::upload_tables_diag(td, tf));
+  ADV_CUDA(adv::upload_tables_implicit(td, tf));
   g_tables_uploaded[device] = true;
   return ADV_OK;
 }
@@ -339,6 +342,16 @@ int check_device(const adv_handle *h)
 }
 } // namespace
 
+namespace adv
+{
+namespace detail
+{
+adv::StageArgs base_args(const adv_handle &h, double t) { return ::base_args(h, t); }
+int            launch(adv_handle *h, const adv::StageArgs &A, cudaStream_t s) { return ::launch(h, A, s); }
+int            check_device(const adv_handle *h) { return ::check_device(h); }
+} // namespace detail
+} // namespace adv
+
 extern "C" {
 
 void adv_config_default(adv_config *c)
@@ -408,6 +421,20 @@ int adv_create(const adv_config *cfg, adv_handle **out)
         }
       if (rc)
         break;
+      {
+        std::vector<float> ff(g.fdm_cell.begin(), g.fdm_cell.end());
+        const size_t       nb = g.fdm_cell.size();
+        if ((e = cudaMalloc(&h->d_fdm_cell_d, nb * sizeof(double))) != cudaSuccess ||
+            (e = cudaMalloc(&h->d_fdm_cell_f, nb * sizeof(float))) != cudaSuccess ||
+            (e = cudaMemcpy(h->d_fdm_cell_d, g.fdm_cell.data(), nb * sizeof(double), cudaMemcpyHostToDevice)) !=
+              cudaSuccess ||
+            (e = cudaMemcpy(h->d_fdm_cell_f, ff.data(), nb * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess)
+          {
+            rc = cuda_fail(e, "FDM cell data");
+            break;
+          }
+        h->device_bytes += nb * (sizeof(double) + sizeof(float));
+      }
       e = cudaMalloc(&h->d_partials, 3 * 4096 * sizeof(double));
       if (e != cudaSuccess)
         {
@@ -438,6 +465,8 @@ int adv_destroy(adv_handle *h)
       cudaFree(h->d_face_x[d]);
     }
   cudaFree(h->d_partials);
+  cudaFree(h->d_fdm_cell_d);
+  cudaFree(h->d_fdm_cell_f);
   cudaFree(h->d_scratch[0]);
   cudaFree(h->d_scratch[1]);
   delete h;
@@ -741,6 +770,36 @@ int adv_copy_from_host(adv_handle *h, const double *host, double *dev, void *str
     return fail(ADV_ERR_INVALID, "null argument");
   ADV_CUDA(cudaMemcpyAsync(dev, host, h->mesh.n_dofs * sizeof(double), cudaMemcpyHostToDevice,
                            (cudaStream_t)stream));
+  return ADV_OK;
+}
+
+int adv_fdm_tables(int degree, double flux_alpha, int sign_index, double *lambda, double *V,
+                   double *VinvW, double *A1, double *residual)
+{
+  if (degree < 1 || degree > 6 || (sign_index != 0 && sign_index != 1))
+    return fail(ADV_ERR_INVALID, "degree must be in 1..6 and sign_index 0 or 1");
+  adv::FdmTables t;
+  if (!adv::fdm_tables(degree, flux_alpha, t))
+    return fail(ADV_ERR_NOT_CONVERGED, "eigen-decomposition of the 1D operator did not converge");
+  const int n = t.n;
+  for (int i = 0; i < n; ++i)
+    {
+      if (lambda)
+        lambda[2 * i] = t.lambda[sign_index][i].real(), lambda[2 * i + 1] = t.lambda[sign_index][i].imag();
+      for (int j = 0; j < n; ++j)
+        {
+          if (V)
+            V[2 * (i * n + j)] = t.V[sign_index][i * n + j].real(),
+                          V[2 * (i * n + j) + 1] = t.V[sign_index][i * n + j].imag();
+          if (VinvW)
+            VinvW[2 * (i * n + j)] = t.VinvW[sign_index][i * n + j].real(),
+                              VinvW[2 * (i * n + j) + 1] = t.VinvW[sign_index][i * n + j].imag();
+          if (A1)
+            A1[i * n + j] = t.A1[sign_index][i * n + j];
+        }
+    }
+  if (residual)
+    *residual = t.residual;
   return ADV_OK;
 }
 

@@ -37,6 +37,8 @@ struct DevTables
   T lw0[kMaxNDev], lw1[kMaxNDev]; // the same divided by the Gauss weights
   T gw[kMaxNDev];                 // Gauss weights
   EvenOdd<T> S_eo, Si_eo, Dw_eo, D_eo;  // S, S^-1 symmetric; Dw, D antisymmetric
+  T St[kMaxNDev][kMaxNDev], SiT[kMaxNDev][kMaxNDev]; // transposes of S and S^-1
+  EvenOdd<T> St_eo, SiT_eo;
   // viscous (SIPG) terms: Gauss-Lagrange derivatives at the faces, the same
   // divided by the weights, nodal-basis derivatives at the faces
   T ld0[kMaxNDev], ld1[kMaxNDev], lwd0[kMaxNDev], lwd1[kMaxNDev], dphi0[kMaxNDev], dphi1[kMaxNDev];

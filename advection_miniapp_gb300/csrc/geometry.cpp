@@ -192,6 +192,17 @@ void compute_geometry(const adv_config &cfg, const Mesh &m, const Tables1D &tb, 
     }
   g.h_min = hmin;
 
+  g.fdm_cell.assign((size_t)m.n_cells * 4, 0.0);
+  if (m.uniform)
+    {
+      const double V = m.h[0] * m.h[1] * m.h[2];
+      for (int64_t c = 0; c < m.n_cells; ++c)
+        {
+          for (int d = 0; d < 3; ++d)
+            g.fdm_cell[4 * c + d] = cfg.velocity[d] / m.h[d];
+          g.fdm_cell[4 * c + 3] = 1.0 / V;
+        }
+    }
   if (m.uniform)
     {
       const double V = m.h[0] * m.h[1] * m.h[2];
@@ -219,15 +230,24 @@ void compute_geometry(const adv_config &cfg, const Mesh &m, const Tables1D &tb, 
             cell_support_points(cfg, m, tb, c, X.data());
             map_grid(n, X.data(), n, S, Sd, n, S, Sd, n, S, Sd, x.data(), J.data());
             double *out = &g.cell[(size_t)c * 4 * nq];
+            double  vavg[3] = {0.0, 0.0, 0.0}, vol = 0.0;
             for (int q = 0; q < nq; ++q)
               {
                 double       Ji[9], b[3];
                 const double det = det_inverse(&J[9 * q], Ji);
                 velocity_field(cfg, &x[3 * q], b);
+                const double w = tb.gw[q % n] * tb.gw[(q / n) % n] * tb.gw[q / (n * n)];
                 for (int d = 0; d < 3; ++d)
-                  out[d * nq + q] = det * (Ji[3 * d + 0] * b[0] + Ji[3 * d + 1] * b[1] + Ji[3 * d + 2] * b[2]);
+                  {
+                    out[d * nq + q] = det * (Ji[3 * d + 0] * b[0] + Ji[3 * d + 1] * b[1] + Ji[3 * d + 2] * b[2]);
+                    vavg[d] += out[d * nq + q] * w;
+                  }
                 out[3 * nq + q] = 1.0 / det;
+                vol += det * w;
               }
+            for (int d = 0; d < 3; ++d)
+              g.fdm_cell[4 * c + d] = vavg[d] / vol;
+            g.fdm_cell[4 * c + 3] = 1.0 / vol;
           }
       }
     }

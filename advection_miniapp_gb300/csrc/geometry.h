@@ -53,6 +53,10 @@ struct HostGeometry
   // Dirichlet: per direction, per face, n^2 points x 3 coordinates (boundary faces only hold data)
   std::vector<double> face_x[3];
   double h_min = 0.0;
+  // per cell (v0, v1, v2, 1/|K|): JxW-weighted cell average of J^{-1} b and the
+  // inverse cell volume (the cell data of the FDM preconditioner,
+  // advection_solver_implicit.cc:1063-1076)
+  std::vector<double> fdm_cell;
 };
 
 // Sine deformation of the box (mesh_type ADV_MESH_DEFORMED).

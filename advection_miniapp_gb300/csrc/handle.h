@@ -1,0 +1,57 @@
+// Private definition of adv_handle and the helpers shared by the C ABI
+// translation units (api.cu, implicit_api.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/advection_gb300.h"
+#include "geometry.h"
+#include "kernels.h"
+#include "tables.h"
+
+struct adv_handle
+{
+  adv_config       cfg;
+  adv::Mesh        mesh;
+  adv::Tables1D    tb;
+  int              device = 0;
+  double           h_min  = 0.0;
+  // uniform-case constants
+  double cv[3] = {}, P[3] = {}, M[3] = {};
+  // device buffers
+  void    *d_cell_geo    = nullptr;
+  void    *d_face_geo[3] = {};
+  double  *d_face_x[3]   = {};
+  double  *d_partials    = nullptr;
+  double  *d_scratch[2]  = {};
+  int64_t  device_bytes  = 0;
+  int64_t  launches      = 0;
+  adv::DiagArgs diag;
+  // per cell (v0, v1, v2, 1/|K|): cell average of J^{-1} a and inverse volume, for the FDM preconditioner
+  double *d_fdm_cell_d = nullptr;
+  float  *d_fdm_cell_f = nullptr;
+};
+
+
+namespace adv
+{
+namespace detail
+{
+int            fail(int code, const std::string &msg);
+int            cuda_fail(cudaError_t e, const char *where);
+adv::StageArgs base_args(const adv_handle &h, double t);
+int            launch(adv_handle *h, const adv::StageArgs &A, cudaStream_t s);
+int            check_device(const adv_handle *h);
+} // namespace detail
+} // namespace adv
+
+#define ADV_CUDA(call)                                   \
+  do                                                     \
+    {                                                    \
+      cudaError_t e_ = (call);                           \
+      if (e_ != cudaSuccess)                             \
+        return adv::detail::cuda_fail(e_, #call);        \
+    }                                                    \
+  while (0)

@@ -1,0 +1,382 @@
+// Implicit time stepping: the GPU counterpart of the reference's implicit
+// operator (AdvectionOperation::vmult, set_time, apply_inverse_mass_matrix,
+// precondition_block_jacobi; advection_solver_implicit.cc:703-762,
+// 1283-1340) and its FGMRES-driven time integrator
+// (advection_solver_implicit.cc:1457-1525), here with BDF2.
+//
+// Linear solver: flexible GMRES(m) with right preconditioning, classical
+// Gram-Schmidt applied twice, FP64 residuals, inner products, orthogonal
+// basis and update; the block-Jacobi FDM preconditioner runs in FP32 or FP64.
+// One host synchronisation per iteration (the new Hessenberg column and the
+// norm come back together).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fdm.h"
+#include "handle.h"
+#include "implicit_kernels.h"
+
+using adv::detail::fail;
+
+struct adv_solver
+{
+  adv_handle *h                 = nullptr;
+  int         restart           = 30;
+  int         precond_precision = 1;
+  int64_t     n                 = 0;
+  double     *V = nullptr, *Z = nullptr, *w = nullptr, *tmp = nullptr, *b = nullptr;
+  double     *d_small    = nullptr; // [coef1 (m+1) | coef2 (m+1) | norm | y (m)]
+  double     *d_partials = nullptr;
+  void       *d_tables   = nullptr;
+  int64_t     bytes      = 0;
+};
+
+namespace
+{
+int alloc(void **p, size_t bytes, int64_t &count)
+{
+  ADV_CUDA(cudaMalloc(p, bytes));
+  count += (int64_t)bytes;
+  return ADV_OK;
+}
+
+int launch_vmult(adv_handle *h, const double *src, double *dst, double mass_factor, double t, cudaStream_t s)
+{
+  adv::StageArgs A = adv::detail::base_args(*h, t);
+  A.mode           = adv::kModeVmult;
+  A.r_in           = src;
+  A.r_out          = dst;
+  A.mass_factor    = mass_factor;
+  A.mass_factorf   = (float)mass_factor;
+  A.vol            = h->mesh.h[0] * h->mesh.h[1] * h->mesh.h[2];
+  A.volf           = (float)A.vol;
+  return adv::detail::launch(h, A, s);
+}
+
+int launch_mass_op(adv_handle *h, const double *src, double *dst, cudaStream_t s)
+{
+  adv::MassArgs A;
+  A.src      = src;
+  A.dst      = dst;
+  A.n_cells  = h->mesh.n_cells;
+  A.uniform  = h->mesh.uniform;
+  A.vol      = h->mesh.h[0] * h->mesh.h[1] * h->mesh.h[2];
+  A.cell_geo = static_cast<const double *>(h->d_cell_geo);
+  ADV_CUDA(adv::launch_mass(h->mesh.n, A, s));
+  ++h->launches;
+  return ADV_OK;
+}
+
+double time_factor_of(const adv_handle &h, double t)
+{
+  return h.cfg.velocity_type == ADV_VELOCITY_CONSTANT ? 1.0 : std::cos(3.14159265358979323846 * t / h.cfg.velocity_period);
+}
+
+int norm2(adv_solver *S, const double *x, double *out, cudaStream_t s)
+{
+  ADV_CUDA(adv::launch_multi_dot(x, 0, 1, x, S->n, S->d_partials, S->d_small + 2 * (S->restart + 1), s));
+  ADV_CUDA(cudaMemcpyAsync(out, S->d_small + 2 * (S->restart + 1), sizeof(double), cudaMemcpyDeviceToHost, s));
+  ADV_CUDA(cudaStreamSynchronize(s));
+  *out = std::sqrt(*out);
+  return ADV_OK;
+}
+} // namespace
+
+extern "C" {
+
+int adv_vmult(adv_handle *h, const double *src, double *dst, double mass_factor, double t, void *stream)
+{
+  if (!h || !src || !dst)
+    return fail(ADV_ERR_INVALID, "null argument");
+  if (src == dst)
+    return fail(ADV_ERR_ALIASING, "adv_vmult: dst must not alias src");
+  if (int e = adv::detail::check_device(h))
+    return e;
+  return launch_vmult(h, src, dst, mass_factor, t, (cudaStream_t)stream);
+}
+
+int adv_apply_mass(adv_handle *h, const double *src, double *dst, void *stream)
+{
+  if (!h || !src || !dst)
+    return fail(ADV_ERR_INVALID, "null argument");
+  if (src == dst)
+    return fail(ADV_ERR_ALIASING, "adv_apply_mass: dst must not alias src");
+  if (!h->mesh.uniform && h->cfg.precision != ADV_PRECISION_FP64)
+    return fail(ADV_ERR_INVALID, "adv_apply_mass needs an FP64 handle on curved meshes or with variable velocity");
+  if (int e = adv::detail::check_device(h))
+    return e;
+  return launch_mass_op(h, src, dst, (cudaStream_t)stream);
+}
+
+int adv_solver_create(adv_handle *h, int restart, int precond_precision, adv_solver **out)
+{
+  if (!h || !out)
+    return fail(ADV_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (restart < 1 || restart > 60)
+    return fail(ADV_ERR_INVALID, "restart must be in 1..60");
+  if (precond_precision != ADV_PRECISION_FP64 && precond_precision != ADV_PRECISION_FP32_OPERATOR)
+    return fail(ADV_ERR_INVALID, "unknown preconditioner precision");
+  if (h->cfg.precision != ADV_PRECISION_FP64)
+    return fail(ADV_ERR_INVALID, "the implicit solver needs an FP64 operator handle (residuals are FP64)");
+  if (h->cfg.diffusion != 0.0)
+    return fail(ADV_ERR_INVALID, "the implicit solver covers advection without diffusion");
+  if (!h->mesh.periodic && h->cfg.boundary_value != ADV_BOUNDARY_ZERO)
+    return fail(ADV_ERR_INVALID, "the implicit solver needs periodic meshes or zero Dirichlet data (a linear operator)");
+  if (int e = adv::detail::check_device(h))
+    return e;
+  adv::FdmTables t;
+  if (!adv::fdm_tables(h->cfg.degree, h->cfg.flux_alpha, t))
+    return fail(ADV_ERR_NOT_CONVERGED, "eigen-decomposition of the 1D operator did not converge");
+  auto *S              = new adv_solver();
+  S->h                 = h;
+  S->restart           = restart;
+  S->precond_precision = precond_precision;
+  S->n                 = h->mesh.n_dofs;
+  const size_t nb      = S->n * sizeof(double);
+  int          rc      = ADV_OK;
+  if ((rc = alloc((void **)&S->V, (restart + 1) * nb, S->bytes)) || (rc = alloc((void **)&S->Z, restart * nb, S->bytes)) ||
+      (rc = alloc((void **)&S->w, nb, S->bytes)) || (rc = alloc((void **)&S->tmp, nb, S->bytes)) ||
+      (rc = alloc((void **)&S->b, nb, S->bytes)) ||
+      (rc = alloc((void **)&S->d_small, (3 * (restart + 1) + 1) * sizeof(double), S->bytes)) ||
+      (rc = alloc((void **)&S->d_partials, adv::vec_partial_blocks(S->n) * (restart + 1) * sizeof(double), S->bytes)))
+    {
+      adv_solver_destroy(S);
+      return rc;
+    }
+  // FDM tables per sign: [VWr VWi Vr Vi lr li]
+  const int           n = t.n, per = 4 * n * n + 2 * n;
+  std::vector<double> tab(2 * per);
+  for (int si = 0; si < 2; ++si)
+    {
+      double *p = tab.data() + si * per;
+      for (int i = 0; i < n * n; ++i)
+        {
+          p[i]             = t.VinvW[si][i].real();
+          p[n * n + i]     = t.VinvW[si][i].imag();
+          p[2 * n * n + i] = t.V[si][i].real();
+          p[3 * n * n + i] = t.V[si][i].imag();
+        }
+      for (int i = 0; i < n; ++i)
+        {
+          p[4 * n * n + i]     = t.lambda[si][i].real();
+          p[4 * n * n + n + i] = t.lambda[si][i].imag();
+        }
+    }
+  if (precond_precision == ADV_PRECISION_FP64)
+    {
+      if ((rc = alloc(&S->d_tables, tab.size() * sizeof(double), S->bytes)) == ADV_OK)
+        if (cudaMemcpy(S->d_tables, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+          rc = fail(ADV_ERR_CUDA, "upload of the FDM tables");
+    }
+  else
+    {
+      std::vector<float> tf(tab.begin(), tab.end());
+      if ((rc = alloc(&S->d_tables, tf.size() * sizeof(float), S->bytes)) == ADV_OK)
+        if (cudaMemcpy(S->d_tables, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+          rc = fail(ADV_ERR_CUDA, "upload of the FDM tables");
+    }
+  if (rc)
+    {
+      adv_solver_destroy(S);
+      return rc;
+    }
+  *out = S;
+  return ADV_OK;
+}
+
+int adv_solver_destroy(adv_solver *S)
+{
+  if (!S)
+    return ADV_OK;
+  cudaFree(S->V);
+  cudaFree(S->Z);
+  cudaFree(S->w);
+  cudaFree(S->tmp);
+  cudaFree(S->b);
+  cudaFree(S->d_small);
+  cudaFree(S->d_partials);
+  cudaFree(S->d_tables);
+  delete S;
+  return ADV_OK;
+}
+
+int adv_solver_device_bytes(const adv_solver *S, int64_t *out)
+{
+  if (!S || !out)
+    return fail(ADV_ERR_INVALID, "null argument");
+  *out = S->bytes;
+  return ADV_OK;
+}
+
+int adv_precondition(adv_solver *S, const double *src, double *dst, double mass_factor, double t, void *stream)
+{
+  if (!S || !src || !dst)
+    return fail(ADV_ERR_INVALID, "null argument");
+  if (src == dst)
+    return fail(ADV_ERR_ALIASING, "adv_precondition: dst must not alias src");
+  adv_handle *h = S->h;
+  if (int e = adv::detail::check_device(h))
+    return e;
+  adv::FdmArgs A;
+  A.src         = src;
+  A.dst         = dst;
+  A.n_cells     = h->mesh.n_cells;
+  A.mass_factor = mass_factor;
+  A.time_factor = time_factor_of(*h, t);
+  const void *cell = S->precond_precision == ADV_PRECISION_FP64 ? (const void *)h->d_fdm_cell_d
+                                                                 : (const void *)h->d_fdm_cell_f;
+  ADV_CUDA(adv::launch_fdm(h->mesh.n, S->precond_precision, A, S->d_tables, cell, (cudaStream_t)stream));
+  ++h->launches;
+  return ADV_OK;
+}
+
+int adv_fgmres(adv_solver *S, double mass_factor, double t, const double *rhs, double *x, double rel_tol,
+               int max_iterations, int *iterations, double *rel_residual, void *stream)
+{
+  if (!S || !rhs || !x)
+    return fail(ADV_ERR_INVALID, "null argument");
+  if (rhs == x)
+    return fail(ADV_ERR_ALIASING, "adv_fgmres: x must not alias rhs");
+  adv_handle *h = S->h;
+  if (int e = adv::detail::check_device(h))
+    return e;
+  cudaStream_t s  = (cudaStream_t)stream;
+  const int    m  = S->restart;
+  const int64_t n = S->n;
+  double      *c1 = S->d_small, *c2 = S->d_small + (m + 1), *nrm = S->d_small + 2 * (m + 1),
+         *ydev = S->d_small + 2 * (m + 1) + 1;
+  double bnorm = 0.0;
+  if (int e = norm2(S, rhs, &bnorm, s))
+    return e;
+  int    its = 0;
+  double res = 0.0;
+  if (bnorm == 0.0)
+    {
+      ADV_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+      if (iterations)
+        *iterations = 0;
+      if (rel_residual)
+        *rel_residual = 0.0;
+      return ADV_OK;
+    }
+  std::vector<double> H((m + 1) * m), cs(m), sn(m), g(m + 1), y(m), hh(2 * (m + 1) + 1);
+  bool                converged = false;
+  while (true)
+    {
+      // r = rhs - A x into V_0
+      if (int e = launch_vmult(h, x, S->w, mass_factor, t, s))
+        return e;
+      ADV_CUDA(adv::launch_lincomb(S->V, 1.0, rhs, -1.0, S->w, n, s));
+      double beta = 0.0;
+      if (int e = norm2(S, S->V, &beta, s))
+        return e;
+      res = beta / bnorm;
+      if (res <= rel_tol)
+        {
+          converged = true;
+          break;
+        }
+      if (its >= max_iterations)
+        break;
+      ADV_CUDA(adv::launch_lincomb(S->V, 1.0 / beta, S->V, 0.0, nullptr, n, s));
+      std::fill(H.begin(), H.end(), 0.0);
+      std::fill(g.begin(), g.end(), 0.0);
+      g[0]  = beta;
+      int k = 0; // columns built in this cycle
+      for (int j = 0; j < m && its < max_iterations; ++j)
+        {
+          double *vj = S->V + j * n, *zj = S->Z + j * n;
+          if (int e = adv_precondition(S, vj, zj, mass_factor, t, stream))
+            return e;
+          if (int e = launch_vmult(h, zj, S->w, mass_factor, t, s))
+            return e;
+          // classical Gram-Schmidt, twice
+          ADV_CUDA(adv::launch_multi_dot(S->V, n, j + 1, S->w, n, S->d_partials, c1, s));
+          ADV_CUDA(adv::launch_multi_axpy(S->w, S->V, n, j + 1, c1, -1.0, n, s));
+          ADV_CUDA(adv::launch_multi_dot(S->V, n, j + 1, S->w, n, S->d_partials, c2, s));
+          ADV_CUDA(adv::launch_multi_axpy(S->w, S->V, n, j + 1, c2, -1.0, n, s));
+          ADV_CUDA(adv::launch_multi_dot(S->w, 0, 1, S->w, n, S->d_partials, nrm, s));
+          ADV_CUDA(cudaMemcpyAsync(hh.data(), S->d_small, (2 * (m + 1) + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
+          ADV_CUDA(cudaStreamSynchronize(s));
+          const double hn = std::sqrt(hh[2 * (m + 1)]);
+          for (int i = 0; i <= j; ++i)
+            H[i * m + j] = hh[i] + hh[(m + 1) + i];
+          H[(j + 1) * m + j] = hn;
+          // Givens rotations
+          for (int i = 0; i < j; ++i)
+            {
+              const double a = H[i * m + j], b = H[(i + 1) * m + j];
+              H[i * m + j]       = cs[i] * a + sn[i] * b;
+              H[(i + 1) * m + j] = -sn[i] * a + cs[i] * b;
+            }
+          const double a = H[j * m + j], b = H[(j + 1) * m + j];
+          const double r = std::hypot(a, b);
+          cs[j]          = r == 0.0 ? 1.0 : a / r;
+          sn[j]          = r == 0.0 ? 0.0 : b / r;
+          H[j * m + j]       = r;
+          H[(j + 1) * m + j] = 0.0;
+          g[j + 1]           = -sn[j] * g[j];
+          g[j]               = cs[j] * g[j];
+          ++its;
+          k   = j + 1;
+          res = std::fabs(g[j + 1]) / bnorm;
+          if (res <= rel_tol || hn == 0.0)
+            break;
+          if (j + 1 < m)
+            ADV_CUDA(adv::launch_lincomb(S->V + (j + 1) * n, 1.0 / hn, S->w, 0.0, nullptr, n, s));
+        }
+      // y = H^{-1} g, x += Z y
+      for (int i = k - 1; i >= 0; --i)
+        {
+          double v = g[i];
+          for (int l = i + 1; l < k; ++l)
+            v -= H[i * m + l] * y[l];
+          y[i] = v / H[i * m + i];
+        }
+      ADV_CUDA(cudaMemcpyAsync(ydev, y.data(), k * sizeof(double), cudaMemcpyHostToDevice, s));
+      ADV_CUDA(adv::launch_multi_axpy(x, S->Z, n, k, ydev, 1.0, n, s));
+      ADV_CUDA(cudaStreamSynchronize(s)); // y lives on the host stack frame
+    }
+  if (iterations)
+    *iterations = its;
+  if (rel_residual)
+    *rel_residual = res;
+  if (!converged)
+    return fail(ADV_ERR_NOT_CONVERGED, "FGMRES reached the iteration limit, relative residual " + std::to_string(res));
+  return ADV_OK;
+}
+
+int adv_bdf2_step(adv_solver *S, double t_new, double dt, int first_step, const double *u_n, const double *u_nm1,
+                  double *u_new, double rel_tol, int *iterations, void *stream)
+{
+  if (!S || !u_n || !u_new || (!first_step && !u_nm1))
+    return fail(ADV_ERR_INVALID, "null argument");
+  if (u_new == u_n || u_new == u_nm1)
+    return fail(ADV_ERR_ALIASING, "u_new must not alias u_n or u_nm1");
+  if (!(dt > 0.0))
+    return fail(ADV_ERR_INVALID, "dt must be positive");
+  adv_handle  *h = S->h;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t n = S->n;
+  double        cm;
+  // right-hand side M tmp: BDF1 on the first step, BDF2 afterwards
+  if (first_step)
+    {
+      cm = 1.0 / dt;
+      ADV_CUDA(adv::launch_lincomb(S->tmp, 1.0 / dt, u_n, 0.0, nullptr, n, s));
+      ADV_CUDA(cudaMemcpyAsync(u_new, u_n, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
+  else
+    {
+      cm = 1.5 / dt;
+      ADV_CUDA(adv::launch_lincomb(S->tmp, 2.0 / dt, u_n, -0.5 / dt, u_nm1, n, s));
+      ADV_CUDA(adv::launch_lincomb(u_new, 2.0, u_n, -1.0, u_nm1, n, s)); // extrapolated initial guess
+    }
+  if (int e = launch_mass_op(h, S->tmp, S->b, s))
+    return e;
+  return adv_fgmres(S, cm, t_new, S->b, u_new, rel_tol, 100000, iterations, nullptr, stream);
+}
+
+} // extern "C"

@@ -12,7 +12,8 @@ enum StageMode
 {
   kModeApply     = 0, // r_out = out_scale * M^{-1} L r_in
   kModeStage     = 1, // u_out = u_in + b k, r_out = u_in + a k
-  kModeLastStage = 2  // u_out = u_in + b k
+  kModeLastStage = 2, // u_out = u_in + b k
+  kModeVmult     = 3  // r_out = mass_factor M r_in - L r_in (weak form, the implicit operator)
 };
 
 // Arguments of the fused stage kernel (one launch = one LSRK stage or one
@@ -47,6 +48,10 @@ struct StageArgs
   double        adv_scale;   // velocity time factor, applied in-kernel when visc != 0
   float         adv_scalef;
   int           pad1;
+  double        mass_factor; // vmult mode: factor of the mass matrix
+  float         mass_factorf;
+  float         volf;        // uniform case: cell volume (det J)
+  double        vol;
   const void   *cell_geo;    // field case: [vt0|vt1|vt2|idet] x n^3 per cell (T)
   const void   *face_geo[3]; // field case: [P|M] x n^2 per face (T)
   const double *face_x[3];   // Dirichlet faces: n^2 x 3 coordinates per face

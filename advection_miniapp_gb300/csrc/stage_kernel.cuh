@@ -74,6 +74,9 @@ struct Consts<double>
   static __device__ __forceinline__ double K2(const StageArgs &A, int d) { return A.K2[d]; }
   static __device__ __forceinline__ double cdiff(const StageArgs &A, int d) { return A.cdiff[d]; }
   static __device__ __forceinline__ double sa(const StageArgs &A) { return A.adv_scale; }
+  static __device__ __forceinline__ double mass(const StageArgs &A) { return A.mass_factor; }
+  static __device__ __forceinline__ double out(const StageArgs &A) { return A.out_scale; }
+  static __device__ __forceinline__ double vol(const StageArgs &A) { return A.vol; }
 };
 template <>
 struct Consts<float>
@@ -86,6 +89,9 @@ struct Consts<float>
   static __device__ __forceinline__ float K2(const StageArgs &A, int d) { return A.K2f[d]; }
   static __device__ __forceinline__ float cdiff(const StageArgs &A, int d) { return A.cdifff[d]; }
   static __device__ __forceinline__ float sa(const StageArgs &A) { return A.adv_scalef; }
+  static __device__ __forceinline__ float mass(const StageArgs &A) { return A.mass_factorf; }
+  static __device__ __forceinline__ float out(const StageArgs &A) { return (float)A.out_scale; }
+  static __device__ __forceinline__ float vol(const StageArgs &A) { return A.volf; }
 };
 
 template <int N, typename T>
@@ -553,14 +559,33 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS)
                                          s_nbr[cl * 6 + 4] < 0, s_nbr[cl * 6 + 5] < 0, r,
                                    F, F + 2 * NF, G + 2 * NQ + r, NF, out);
       T *z = Qb + cl * NQ + r;
-#pragma unroll
-      for (int k = 0; k < N; ++k)
+      if (A.mode != kModeVmult)
         {
-          zz[k] = z[k * NF] + out[k];
-          if (!UNI)
-            zz[k] *= G[3 * NQ + r + k * NF];
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            {
+              zz[k] = z[k * NF] + out[k];
+              if (!UNI)
+                zz[k] *= G[3 * NQ + r + k * NF];
+            }
+          sweep2<N, T, false>(tb.Si, tb.Si_eo, zz, kk);
         }
-      sweep2<N, T, false>(tb.Si, tb.Si_eo, zz, kk);
+      else
+        {
+          // implicit operator in weak form: S^T [JxW (c U - Z)], with
+          // JxW Z = w B (field) or w V B (uniform) for the bracket B
+          const T cm = Consts<T>::mass(A), sc = Consts<T>::out(A);
+          const T wxy = tb.gw[r % N] * tb.gw[r / N];
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            {
+              const T bracket = sc * (z[k * NF] + out[k]);
+              const T wq      = wxy * tb.gw[k];
+              zz[k] = UNI ? wq * Consts<T>::vol(A) * (cm * U[k] - bracket)
+                          : wq * (cm * U[k] / G[3 * NQ + r + k * NF] - bracket);
+            }
+          sweep2<N, T, false>(tb.St, tb.St_eo, zz, kk);
+        }
 #pragma unroll
       for (int k = 0; k < N; ++k)
         z[k * NF] = kk[k];
@@ -576,7 +601,10 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS)
 #pragma unroll
       for (int k = 0; k < N; ++k)
         in[k] = p[k * N];
-      sweep2<N, T, false>(tb.Si, tb.Si_eo, in, out);
+      if (A.mode != kModeVmult)
+        sweep2<N, T, false>(tb.Si, tb.Si_eo, in, out);
+      else
+        sweep2<N, T, false>(tb.St, tb.St_eo, in, out);
 #pragma unroll
       for (int k = 0; k < N; ++k)
         p[k * N] = out[k];
@@ -591,7 +619,10 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS)
 #pragma unroll
       for (int k = 0; k < N; ++k)
         in[k] = p[k];
-      sweep2<N, T, false>(tb.Si, tb.Si_eo, in, out);
+      if (A.mode != kModeVmult)
+        sweep2<N, T, false>(tb.Si, tb.Si_eo, in, out);
+      else
+        sweep2<N, T, false>(tb.St, tb.St_eo, in, out);
 #pragma unroll
       for (int k = 0; k < N; ++k)
         p[k] = out[k];
@@ -601,7 +632,12 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS)
   // ---- phase 8: Runge-Kutta update over the CTA's contiguous DoF range
   //      (the post-operation lambda of advection_solver.cc:728-752)
   const long long g0 = cell0 * NQ;
-  if (A.mode == kModeApply)
+  if (A.mode == kModeVmult)
+    {
+      for (int i = tid; i < ncell * NQ; i += NT)
+        A.r_out[g0 + i] = to_double<T>(Qb[i]);
+    }
+  else if (A.mode == kModeApply)
     {
       for (int i = tid; i < ncell * NQ; i += NT)
         A.r_out[g0 + i] = A.out_scale * to_double<T>(Qb[i]);

@@ -148,6 +148,50 @@ int adv_time_step(adv_handle *h, double courant, double *dt);
 int adv_copy_to_host(adv_handle *h, const double *dev, double *host, void *stream);
 int adv_copy_from_host(adv_handle *h, const double *host, double *dev, void *stream);
 
+/* ------------------------------------------------------------ implicit solver
+ * The implicit operator of advection_solver_implicit.cc: vmult = M/dt + A
+ * (:703-726, 821-887) with A = -L the left-hand-side advection operator, the
+ * inverse mass matrix, the block-Jacobi fast-diagonalization preconditioner
+ * (precondition_block_jacobi, :1283-1340) and an FGMRES solver (SolverFGMRES,
+ * :1498-1504) driving BDF2 time steps.  FP64 residuals, inner products,
+ * orthogonalisation and updates; the preconditioner in FP32 or FP64. */
+typedef struct adv_solver adv_solver;
+
+/* AdvectionOperation::vmult: dst = mass_factor * M src - L(t) src (weak form). */
+int adv_vmult(adv_handle *h, const double *src, double *dst, double mass_factor, double t, void *stream);
+/* dst = M src, the cellwise mass matrix (QGauss(k+1)). */
+int adv_apply_mass(adv_handle *h, const double *src, double *dst, void *stream);
+/* Workspace of FGMRES(restart) (restart + 1 basis and restart preconditioned
+ * vectors) and the FDM tables; precond_precision is ADV_PRECISION_FP64 or
+ * ADV_PRECISION_FP32_OPERATOR.  Needs an FP64 handle without diffusion and a
+ * linear operator (periodic, or zero Dirichlet data). */
+int adv_solver_create(adv_handle *h, int restart, int precond_precision, adv_solver **out);
+int adv_solver_destroy(adv_solver *s);
+int adv_solver_device_bytes(const adv_solver *s, int64_t *out);
+/* Block-Jacobi FDM preconditioner: dst ~ (mass_factor M - L_cell(t))^{-1} src,
+ * cell by cell (CellwisePreconditionerFDM, advection_solver_implicit.cc:490-646). */
+int adv_precondition(adv_solver *s, const double *src, double *dst, double mass_factor, double t, void *stream);
+/* Solves (mass_factor M - L(t)) x = rhs with right-preconditioned flexible
+ * GMRES from the initial guess in x, to ||rhs - A x|| <= rel_tol ||rhs||.
+ * Returns ADV_ERR_NOT_CONVERGED after max_iterations. */
+int adv_fgmres(adv_solver *s, double mass_factor, double t, const double *rhs, double *x, double rel_tol,
+               int max_iterations, int *iterations, double *rel_residual, void *stream);
+/* One BDF2 step to time t_new: (3 u_new - 4 u_n + u_nm1) / (2 dt) = M^{-1} L(t_new) u_new
+ * (first_step != 0: implicit Euler, u_nm1 unused), initial guess 2 u_n - u_nm1. */
+int adv_bdf2_step(adv_solver *s, double t_new, double dt, int first_step, const double *u_n, const double *u_nm1,
+                  double *u_new, double rel_tol, int *iterations, void *stream);
+
+/* 1D fast-diagonalization tables of the cellwise preconditioner (the 1D set-up
+ * of advection_solver_implicit.cc:1020-1062): on the unit interval with the
+ * Lagrange basis on the k+1 Gauss points, W^{-1} A1 = V diag(lambda) V^{-1}
+ * for unit velocity of sign +1 (sign_index 0) or -1 (sign_index 1).  Complex
+ * outputs are interleaved (re, im): lambda[2n], V[2n^2] and VinvW[2n^2]
+ * (= V^{-1} W^{-1}) row-major; A1[n^2] is the real matrix W^{-1} A1;
+ * residual = max |W^{-1}A1 V - V Lambda| / max |W^{-1}A1| over both signs.
+ * Any output pointer may be NULL.  Host only. */
+int adv_fdm_tables(int degree, double flux_alpha, int sign_index, double *lambda, double *V,
+                   double *VinvW, double *A1, double *residual);
+
 /* Number of kernel launches the library has issued on this handle. */
 int adv_launch_count(const adv_handle *h, int64_t *out);
 

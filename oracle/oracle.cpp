@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstring>
 #include <memory>
 #include <vector>
@@ -1236,6 +1237,126 @@ void dispatch(int n, Args &&...args)
     }
 }
 
+// cellwise mass matrix S^T diag(JxW) S
+template <int N>
+struct RunMass
+{
+  static void run(const Op &op, const double *src, double *dst)
+  {
+    constexpr int NQ = N * N * N;
+    const Tables &tb = op.tb;
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < op.n_cells; ++c)
+      {
+        double t1[NQ], t2[NQ];
+        apply3<N, 0, false, false>(tb.S, src + c * NQ, t1);
+        apply3<N, 1, false, false>(tb.S, t1, t2);
+        apply3<N, 2, false, false>(tb.S, t2, t1);
+        for (int q = 0; q < NQ; ++q)
+          t1[q] *= op.jxw[c * NQ + q];
+        apply3<N, 0, true, false>(tb.S, t1, t2);
+        apply3<N, 1, true, false>(tb.S, t2, t1);
+        apply3<N, 2, true, false>(tb.S, t1, dst + c * NQ);
+      }
+  }
+};
+
+// CellwisePreconditionerFDM (advection_solver_implicit.cc:490-646) inside the
+// block-Jacobi loop of precondition_block_jacobi (:1283-1340)
+template <int N>
+struct RunFdm
+{
+  static void run(const Op &op, const double *lam, const double *Vt, const double *VWt, const double *src,
+                  double *dst, double mass_factor)
+  {
+    using cd         = std::complex<double>;
+    constexpr int NQ = N * N * N;
+    const Tables &tb = op.tb;
+    cd            L[2][N], V[2][N][N], VW[2][N][N];
+    for (int s = 0; s < 2; ++s)
+      for (int i = 0; i < N; ++i)
+        {
+          L[s][i] = cd(lam[s * 2 * N + 2 * i], lam[s * 2 * N + 2 * i + 1]);
+          for (int j = 0; j < N; ++j)
+            {
+              V[s][i][j]  = cd(Vt[s * 2 * N * N + 2 * (i * N + j)], Vt[s * 2 * N * N + 2 * (i * N + j) + 1]);
+              VW[s][i][j] = cd(VWt[s * 2 * N * N + 2 * (i * N + j)], VWt[s * 2 * N * N + 2 * (i * N + j) + 1]);
+            }
+        }
+#pragma omp parallel for schedule(static)
+    for (int64_t c = 0; c < op.n_cells; ++c)
+      {
+        // average contravariant velocity and volume of the cell
+        double v[3] = {0, 0, 0}, vol = 0.0;
+        for (int q = 0; q < NQ; ++q)
+          {
+            const double *Ji = &op.jinv[(c * NQ + q) * 9];
+            double        a[3];
+            op.ph.speed(&op.xq[(c * NQ + q) * 3], 0.0, a);
+            const double JxW = op.jxw[c * NQ + q];
+            for (int d = 0; d < 3; ++d)
+              v[d] += (Ji[d * 3 + 0] * a[0] + Ji[d * 3 + 1] * a[1] + Ji[d * 3 + 2] * a[2]) * JxW;
+            vol += JxW;
+          }
+        int sg[3];
+        for (int d = 0; d < 3; ++d)
+          {
+            v[d] /= vol;
+            sg[d] = v[d] < 0.0 ? 1 : 0;
+          }
+        // residual to the collocation basis: S^{-T}
+        double t1[NQ], t2[NQ];
+        apply3<N, 0, true, false>(tb.Si, src + c * NQ, t1);
+        apply3<N, 1, true, false>(tb.Si, t1, t2);
+        apply3<N, 2, true, false>(tb.Si, t2, t1);
+        cd x[NQ], y[NQ];
+        for (int q = 0; q < NQ; ++q)
+          x[q] = t1[q];
+        // V^{-1} W^{-1} in each direction
+        for (int d = 0; d < 3; ++d)
+          {
+            const int st = d == 0 ? 1 : d == 1 ? N : N * N;
+            for (int q = 0; q < NQ; ++q)
+              {
+                const int id = (q / st) % N, base = q - id * st;
+                cd        s  = 0.0;
+                for (int k = 0; k < N; ++k)
+                  s += VW[sg[d]][id][k] * x[base + k * st];
+                y[q] = s;
+              }
+            std::copy(y, y + NQ, x);
+          }
+        for (int q = 0; q < NQ; ++q)
+          {
+            const int ii[3] = {q % N, (q / N) % N, q / (N * N)};
+            cd        diag  = mass_factor;
+            for (int d = 0; d < 3; ++d)
+              diag += v[d] * L[sg[d]][ii[d]];
+            x[q] *= (1.0 / vol) / diag;
+          }
+        for (int d = 0; d < 3; ++d)
+          {
+            const int st = d == 0 ? 1 : d == 1 ? N : N * N;
+            for (int q = 0; q < NQ; ++q)
+              {
+                const int id = (q / st) % N, base = q - id * st;
+                cd        s  = 0.0;
+                for (int k = 0; k < N; ++k)
+                  s += V[sg[d]][id][k] * x[base + k * st];
+                y[q] = s;
+              }
+            std::copy(y, y + NQ, x);
+          }
+        for (int q = 0; q < NQ; ++q)
+          t1[q] = x[q].real();
+        // back to the nodal basis: S^{-1}
+        apply3<N, 0, false, false>(tb.Si, t1, t2);
+        apply3<N, 1, false, false>(tb.Si, t2, t1);
+        apply3<N, 2, false, false>(tb.Si, t1, dst + c * NQ);
+      }
+  }
+};
+
 template <int N> struct RunApply { static void run(const Op &op, const double *s, double *d, double t) { Kernels<N>::apply_unscaled(op, s, d, t); } };
 template <int N> struct RunInvMass { static void run(const Op &op, const double *s, double *d) { Kernels<N>::inverse_mass(op, s, d); } };
 template <int N> struct RunProject { static void run(const Op &op, double t, double *d) { Kernels<N>::project(op, t, d); } };
@@ -1507,6 +1628,37 @@ int oracle_interpolate(oracle_op *h, double t, double *dst)
           dst[c * nq + i] = op.ph.exact(&X[3 * i], t);
       }
   }
+  return 0;
+}
+
+int oracle_apply_mass(oracle_op *h, const double *src, double *dst)
+{
+  if (src == dst)
+    return 2;
+  dispatch<RunMass>(h->op.n, h->op, src, dst);
+  return 0;
+}
+
+int oracle_vmult(oracle_op *h, const double *src, double *dst, double mass_factor, double t)
+{
+  if (src == dst)
+    return 2;
+  const int64_t nd = h->op.n_dofs;
+  h->tmp.resize(nd);
+  dispatch<RunApply>(h->op.n, h->op, src, h->tmp.data(), t);
+  dispatch<RunMass>(h->op.n, h->op, src, dst);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < nd; ++i)
+    dst[i] = mass_factor * dst[i] - h->tmp[i];
+  return 0;
+}
+
+int oracle_fdm_apply(oracle_op *h, const double *lambda, const double *V, const double *VinvW,
+                     const double *src, double *dst, double mass_factor)
+{
+  if (src == dst)
+    return 2;
+  dispatch<RunFdm>(h->op.n, h->op, lambda, V, VinvW, src, dst, mass_factor);
   return 0;
 }
 

@@ -104,6 +104,24 @@ int oracle_interpolate(oracle_op *op, double t, double *dst);
 /* Physical coordinates of every DoF's support point (3 doubles per DoF). */
 int oracle_support_points(oracle_op *op, double *xyz);
 
+/* Implicit solver pieces (advection_solver_implicit.cc).
+ * dst = M src (cellwise mass matrix, QGauss(k+1)). */
+int oracle_apply_mass(oracle_op *op, const double *src, double *dst);
+/* vmult (advection_solver_implicit.cc:710-726): dst = mass_factor M src - L(t) src,
+ * i.e. M/dt + A with A the left-hand-side advection operator. */
+int oracle_vmult(oracle_op *op, const double *src, double *dst, double mass_factor, double t);
+/* Block-Jacobi with the cellwise fast-diagonalization preconditioner
+ * (CellwisePreconditionerFDM::vmult, advection_solver_implicit.cc:490-646, and
+ * precondition_block_jacobi, :1283-1340): per cell, transform the residual to
+ * the collocation basis on the Gauss points (S^{-T}), apply V^{-1}W^{-1} in
+ * every direction, divide by (1/volume) / (mass_factor + sum_d v_d lambda_d),
+ * apply V, take the real part and transform back (S^{-1}).  v is the cell
+ * average of J^{-1} a (weighted by JxW); the tables of the sign of v_d are used.
+ * Tables (interleaved re, im): lambda[2][2n], V[2][2n^2], VinvW[2][2n^2], index
+ * 0 for positive, 1 for negative velocity. */
+int oracle_fdm_apply(oracle_op *op, const double *lambda, const double *V, const double *VinvW,
+                     const double *src, double *dst, double mass_factor);
+
 /* Second, independent implementation with dense per-cell matrices: basis
  * evaluated at every 3D quadrature point, dense face matrices and a Cholesky
  * solve with the assembled cell mass matrix.  Slow; used to cross-check. */

@@ -83,6 +83,9 @@ def lib():
         L.oracle_min_vertex_distance.argtypes = [P]
         L.oracle_min_vertex_distance.restype = D
         L.oracle_support_points.argtypes = [P, dp]
+        L.oracle_apply_mass.argtypes = [P, dp, dp]
+        L.oracle_vmult.argtypes = [P, dp, dp, D, D]
+        L.oracle_fdm_apply.argtypes = [P, dp, dp, dp, dp, dp, D]
         _lib = L
     return _lib
 
@@ -222,6 +225,24 @@ class Oracle:
 
     def min_vertex_distance(self):
         return lib().oracle_min_vertex_distance(self._h)
+
+    def apply_mass(self, src):
+        dst = self.zeros()
+        assert lib().oracle_apply_mass(self._h, _ptr(src), _ptr(dst)) == 0
+        return dst
+
+    def vmult(self, src, mass_factor, t=0.0):
+        """mass_factor M src - L(t) src (the implicit operator M/dt + A)."""
+        dst = self.zeros()
+        assert lib().oracle_vmult(self._h, _ptr(src), _ptr(dst), mass_factor, t) == 0
+        return dst
+
+    def fdm_apply(self, tables, src, mass_factor):
+        """Block-Jacobi FDM preconditioner with tables = (lambda[2,n], V[2,n,n], VinvW[2,n,n]) complex."""
+        lam, V, VW = (np.ascontiguousarray(np.stack([a.real, a.imag], axis=-1).reshape(-1)) for a in tables)
+        dst = self.zeros()
+        assert lib().oracle_fdm_apply(self._h, _ptr(lam), _ptr(V), _ptr(VW), _ptr(src), _ptr(dst), mass_factor) == 0
+        return dst
 
     def support_points(self):
         xyz = np.zeros(self.n_dofs * 3)

@@ -1,0 +1,107 @@
+"""Implicit path on the GPU against the oracle: the operator M/dt + A
+(vmult), the mass matrix, the block-Jacobi FDM preconditioner, FGMRES (its
+residual re-checked by the oracle) and BDF2 steps with the preconditioner in
+FP64 and FP32."""
+import numpy as np
+import pytest
+
+from test_oracle_implicit import numpy_fdm_tables
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "curved-k4": dict(degree=4, n_cells=(4, 3, 4), mesh_type=1, deformation=0.08),
+    "affine-k3": dict(degree=3, n_cells=(3, 4, 3), velocity=(-0.3, 0.7, 0.4)),
+    "affine-k2-dirichlet": dict(degree=2, n_cells=(3, 3, 3), periodic=0, boundary_value=0),
+    "rotating-k3": dict(degree=3, n_cells=(3, 3, 3), periodic=0, velocity_type=1, velocity=(1.0, 1.0, 0.3),
+                        velocity_period=0.5, initial_condition=1, ic_params=(0.3, 0.5, 0.5, 0.2), boundary_value=0),
+}
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def rel(a, b):
+    a = a.cpu().numpy() if hasattr(a, "cpu") else a
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_vmult_and_mass(cuda, oracle_mod, adv_lib, case):
+    torch = cuda
+    o = oracle_mod.Oracle(**CASES[case])
+    g = adv_lib.AdvectionOperation(**CASES[case])
+    u = np.random.default_rng(3).standard_normal(o.n_dofs)
+    d = g.initialize_dof_vector()
+    g.apply_mass(dev(torch, u), d)
+    assert rel(d, o.apply_mass(u)) <= 1e-13
+    for cm, t in ((12.5, 0.0), (3.0, 0.4)):
+        g.vmult(dev(torch, u), d, cm, t)
+        assert rel(d, o.vmult(u, cm, t)) <= 1e-12
+
+
+@pytest.mark.parametrize("case", ["curved-k4", "affine-k3", "rotating-k3"])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_fdm_preconditioner(cuda, oracle_mod, adv_lib, case, precision):
+    torch = cuda
+    cfg = CASES[case]
+    o = oracle_mod.Oracle(**cfg)
+    g = adv_lib.AdvectionOperation(**cfg)
+    s = adv_lib.ImplicitSolver(g, restart=4, precond_precision=precision)
+    r = np.random.default_rng(4).standard_normal(o.n_dofs)
+    ref = o.fdm_apply(numpy_fdm_tables(oracle_mod, cfg["degree"], 1.0), r, 9.0)
+    d = g.initialize_dof_vector()
+    s.precondition(dev(torch, r), d, 9.0, 0.0)
+    assert rel(d, ref) <= (1e-10 if precision == 0 else 1e-4)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_fgmres_residual_checked_by_oracle(cuda, oracle_mod, adv_lib, precision):
+    torch = cuda
+    cfg = CASES["curved-k4"]
+    o = oracle_mod.Oracle(**cfg)
+    g = adv_lib.AdvectionOperation(**cfg)
+    s = adv_lib.ImplicitSolver(g, restart=10, precond_precision=precision)
+    dt = 8 * o.time_step(1.0) * 0.5
+    cm = 1.5 / dt
+    b = o.apply_mass(np.random.default_rng(5).standard_normal(o.n_dofs))
+    x = g.initialize_dof_vector()
+    its, res = s.fgmres(cm, 0.0, dev(torch, b), x, rel_tol=1e-10, max_iterations=500)
+    xs = x.cpu().numpy()
+    true_res = np.linalg.norm(b - o.vmult(xs, cm)) / np.linalg.norm(b)
+    assert res <= 1e-10 and true_res <= 2e-10, (its, res, true_res)
+    assert its < 200
+
+
+def test_bdf2_steps_and_preconditioner_precision(cuda, oracle_mod, adv_lib):
+    """BDF2 at Courant 8 on a small curved mesh: every step solves its system
+    (checked by the oracle), FP32 and FP64 preconditioners give the same
+    solution to the solver tolerance, and the solution tracks the exact one."""
+    torch = cuda
+    cfg = dict(degree=4, n_cells=(6, 6, 6), mesh_type=1, deformation=0.08)
+    o = oracle_mod.Oracle(**cfg)
+    g = adv_lib.AdvectionOperation(**cfg)
+    dt = g.time_step(8.0)
+    finals, iters = {}, {}
+    for precision in (0, 1):
+        s = adv_lib.ImplicitSolver(g, restart=30, precond_precision=precision)
+        u_nm1 = g.initialize_dof_vector()
+        u_n = g.initialize_dof_vector()
+        g.project_initial(u_n)
+        u_new = g.initialize_dof_vector()
+        its = []
+        for step in range(6):
+            its.append(s.bdf2_step((step + 1) * dt, dt, step == 0, u_n, u_nm1, u_new, rel_tol=1e-10))
+            if step == 2:
+                # the oracle re-checks this step's linear system
+                un, unm1, unew = u_n.cpu().numpy(), u_nm1.cpu().numpy(), u_new.cpu().numpy()
+                cm = 1.5 / dt
+                b = o.apply_mass((2.0 * un - 0.5 * unm1) / dt)
+                assert np.linalg.norm(b - o.vmult(unew, cm)) / np.linalg.norm(b) <= 2e-10
+            u_nm1, u_n, u_new = u_n, u_new, u_nm1
+        finals[precision] = u_n.cpu().numpy()
+        iters[precision] = its
+    assert rel(finals[1], finals[0]) <= 1e-8, iters
+    err, nrm = g.l2_error(dev(torch, finals[0]), 6 * dt)
+    assert err / nrm < 0.05, err / nrm
