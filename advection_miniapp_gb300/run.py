@@ -40,7 +40,51 @@ def parse(argv=None):
     p.add_argument("--skew", type=float, default=0.0)
     p.add_argument("--output-every", type=int, default=0, help="0: only at the start and the end")
     p.add_argument("--json", action="store_true", help="print one JSON summary line")
+    p.add_argument("--implicit", action="store_true",
+                   help="BDF2 steps with FGMRES and the block-Jacobi FDM preconditioner instead of LSRK")
+    p.add_argument("--restart", type=int, default=30, help="FGMRES restart length (implicit)")
+    p.add_argument("--tolerance", type=float, default=1e-10, help="FGMRES relative tolerance (implicit)")
+    p.add_argument("--precond-precision", choices=["fp64", "fp32"], default="fp32",
+                   help="precision of the FDM preconditioner (implicit)")
+    p.add_argument("--compare-fp64-precond", action="store_true",
+                   help="implicit: rerun with the FP64 preconditioner and report the difference")
     return p.parse_args(argv)
+
+
+def run_implicit(args, op):
+    """BDF2 + FGMRES: the implicit workload (advection_solver_implicit.cc:1788-1886 with BDF2)."""
+    import time as _time
+
+    from . import ImplicitSolver, PRECISION_FP32_OPERATOR, PRECISION_FP64
+
+    dt = op.time_step(args.courant)
+
+    def solve(precond):
+        s = ImplicitSolver(op, restart=args.restart, precond_precision=precond)
+        u_nm1, u_n, u_new = (op.initialize_dof_vector() for _ in range(3))
+        op.project_initial(u_n)
+        its = []
+        torch.cuda.synchronize()
+        t0 = _time.perf_counter()
+        for step in range(args.steps):
+            its.append(s.bdf2_step((step + 1) * dt, dt, step == 0, u_n, u_nm1, u_new, rel_tol=args.tolerance))
+            u_nm1, u_n, u_new = u_n, u_new, u_nm1
+        torch.cuda.synchronize()
+        return u_n, its, _time.perf_counter() - t0
+
+    prec = PRECISION_FP32_OPERATOR if args.precond_precision == "fp32" else PRECISION_FP64
+    u, its, wall = solve(prec)
+    err, nrm = op.l2_error(u, args.steps * dt)
+    out = {"n_dofs": op.n_dofs, "steps": args.steps, "dt": dt, "t_end": args.steps * dt, "courant": args.courant,
+           "precond_precision": args.precond_precision, "iterations_per_step": sum(its) / len(its),
+           "iterations": its, "rel_l2_error": err / nrm, "s_per_step": wall / args.steps}
+    if args.compare_fp64_precond:
+        u64, its64, _ = solve(PRECISION_FP64)
+        e64, n64 = op.l2_error(u64, args.steps * dt)
+        d = (u - u64)
+        out["fp64_precond"] = {"iterations_per_step": sum(its64) / len(its64), "rel_l2_error": e64 / n64,
+                               "max_rel_difference": float(d.abs().max() / u64.abs().max())}
+    return out
 
 
 def main(argv=None):
@@ -52,6 +96,14 @@ def main(argv=None):
                       flux_alpha=args.flux_alpha, factor_skew=args.skew,
                       precision=PRECISION_FP64 if args.precision == "fp64" else PRECISION_FP32_OPERATOR)
     op = AdvectionOperation(cfg)
+    if args.implicit:
+        res = run_implicit(args, op)
+        if args.json:
+            print(json.dumps(res))
+        else:
+            for k, v in res.items():
+                print(f"   {k}: {v}")
+        return
     integ = LowStorageRungeKuttaIntegrator(SCHEMES[args.scheme])
     dt = op.time_step(args.courant)
     if not args.json:
