@@ -18,6 +18,7 @@
 #include "fdm.h"
 #include "geometry.h"
 #include "handle.h"
+#include "batch_kernels.h"
 #include "implicit_kernels.h"
 #include "kernels.h"
 #include "tables.h"
@@ -148,6 +149,7 @@ int ensure_tables(int device)
   ADV_CUDA(adv::upload_tables_stage32(td, tf));
   ADV_CUDA(adv::upload_tables_diag(td, tf));
   ADV_CUDA(adv::upload_tables_implicit(td, tf));
+  ADV_CUDA(adv::upload_tables_batch(td, tf));
   g_tables_uploaded[device] = true;
   return ADV_OK;
 }
@@ -206,10 +208,19 @@ int upload_array(const std::vector<double> &src, void **dst, int64_t &bytes)
 
 void fill_diag(adv_handle &h)
 {
-  adv::DiagArgs &g = h.diag;
+  adv::detail::make_diag(h.cfg, h.mesh, h.tb, h.diag);
+}
+} // namespace
+
+void adv::detail::make_diag(const adv_config &cfg, const adv::Mesh &m, const adv::Tables1D &tb, adv::DiagArgs &g)
+{
+  struct
+  {
+    const adv_config    &cfg;
+    const adv::Tables1D &tb;
+  } h{cfg, tb};
   std::memset(&g, 0, sizeof(g));
-  const adv::Mesh &m = h.mesh;
-  const int        n = m.n;
+  const int n = m.n;
   g.n                = n;
   for (int d = 0; d < 3; ++d)
     {
@@ -249,6 +260,9 @@ void fill_diag(adv_handle &h)
         g.SEd[p * n + i] = adv::lagrange_derivative(h.tb.gl, n, i, g.ep[p]);
       }
 }
+
+namespace
+{
 
 // velocity time factor of the rotating field at time t (1 for a constant velocity)
 double time_factor(const adv_handle &h, double t)
@@ -349,6 +363,7 @@ namespace detail
 adv::StageArgs base_args(const adv_handle &h, double t) { return ::base_args(h, t); }
 int            launch(adv_handle *h, const adv::StageArgs &A, cudaStream_t s) { return ::launch(h, A, s); }
 int            check_device(const adv_handle *h) { return ::check_device(h); }
+int            ensure_tables(int device) { return ::ensure_tables(device); }
 } // namespace detail
 } // namespace adv
 

@@ -44,6 +44,10 @@ int            cuda_fail(cudaError_t e, const char *where);
 adv::StageArgs base_args(const adv_handle &h, double t);
 int            launch(adv_handle *h, const adv::StageArgs &A, cudaStream_t s);
 int            check_device(const adv_handle *h);
+// uploads the 1D tables to every translation unit on this device (once)
+int            ensure_tables(int device);
+// arguments of the projection / mass-energy / L2-error kernels for a mesh
+void           make_diag(const adv_config &cfg, const adv::Mesh &m, const adv::Tables1D &tb, adv::DiagArgs &g);
 } // namespace detail
 } // namespace adv
 

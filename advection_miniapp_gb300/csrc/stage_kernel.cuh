@@ -280,16 +280,17 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
     }
 }
 
+// One CTA's work: cells cell0 .. cell0 + C - 1 of the mesh described by A,
+// with the dynamic shared memory of the launch.  Shared by the single-mesh
+// kernel and the batched multi-mesh kernel of the serving loop.
 template <int N, typename T, bool UNI, bool VISC>
-__global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS)
-  stage_kernel(const StageArgs A)
+__device__ __forceinline__ void stage_cta(const StageArgs &A, const long long cell0, unsigned char *smem_raw)
 {
   using SH         = StageShape<N, T, UNI, VISC>;
   constexpr int C  = SH::C;
   constexpr int NQ = SH::NQ;
   constexpr int NF = SH::NF;
   constexpr int NT = SH::THREADS;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   T   *Ub     = reinterpret_cast<T *>(smem_raw); // [C][NQ] nodal -> Gauss values
   T   *Qb     = Ub + C * NQ;                     // [C][NQ] accumulated Z, then k
   T   *Nb     = Qb + C * NQ;                     // [C][6][NF] neighbour face values
@@ -301,7 +302,6 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS)
 
   const DevTables<T> &tb    = tab<T>(N);
   const int           tid   = threadIdx.x;
-  const long long     cell0 = (long long)blockIdx.x * C;
   const int           ncell = (int)min((long long)C, A.n_cells - cell0);
 
   // ---- phase 0a: neighbour cells and face ids of the CTA's cells
@@ -657,6 +657,14 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS)
       for (int i = tid; i < ncell * NQ; i += NT)
         A.u_out[g0 + i] = fma(A.b, to_double<T>(Qb[i]), __ldcs(A.u_in + g0 + i));
     }
+}
+
+template <int N, typename T, bool UNI, bool VISC>
+__global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS)
+  stage_kernel(const StageArgs A)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  stage_cta<N, T, UNI, VISC>(A, (long long)blockIdx.x * StageShape<N, T, UNI, VISC>::C, smem_raw);
 }
 
 template <int N, typename T, bool UNI, bool VISC>

@@ -181,6 +181,38 @@ int adv_fgmres(adv_solver *s, double mass_factor, double t, const double *rhs, d
 int adv_bdf2_step(adv_solver *s, double t_new, double dt, int first_step, const double *u_n, const double *u_nm1,
                   double *u_new, double rel_tol, int *iterations, void *stream);
 
+/* ------------------------------------------------------------- serving loop
+ * Continuous batching of independent solves on one GPU (no counterpart in the
+ * reference, which runs one solve per program).  Requests (periodic affine n^3
+ * meshes, constant velocity, any degree 1..6 and either precision) are admitted
+ * FIFO while their three FP64 vectors fit memory_budget_bytes and at most
+ * max_active solves run; solves of one (degree, precision) share batched
+ * stage launches captured as a CUDA graph of steps_per_tick LSRK(5,4) steps
+ * and replayed while solves join and leave; groups run on their own streams.
+ * Each request's time step follows setup_dofs (advection_solver.cc:1155-1167):
+ * dt = courant h / |a| / k^1.5 rounded to t_end / ceil(t_end / dt).  The
+ * server is not thread-safe. */
+typedef struct adv_server adv_server;
+
+int adv_server_create(int64_t memory_budget_bytes, int steps_per_tick, int max_active, int keep_solutions,
+                      adv_server **out);
+int adv_server_destroy(adv_server *s);
+/* Queues a solve of cfg (its initial condition) to t_end. */
+int adv_server_submit(adv_server *s, const adv_config *cfg, double t_end, double courant, int64_t *request_id);
+/* One scheduling round (non-blocking on the GPU): retire finished solves
+ * (relative L2 error against the exact solution), admit queued ones, start the
+ * next tick of idle groups.  *n_completed: solves retired in this round. */
+int adv_server_poll(adv_server *s, int *n_completed);
+/* Polls until every submitted request is complete. */
+int adv_server_drain(adv_server *s);
+/* state: 0 queued, 1 running, 2 done; latency from submission to retirement. */
+int adv_server_result(adv_server *s, int64_t request_id, int *state, double *rel_l2_error, double *latency_s,
+                      int *steps, double *dt);
+/* Final solution of a done request (servers created with keep_solutions != 0). */
+int adv_server_solution(adv_server *s, int64_t request_id, double *host_out, int64_t n);
+/* out[8] = {submitted, queued, running, completed, device bytes in use, budget, ticks, kernel launches}. */
+int adv_server_stats(const adv_server *s, int64_t *out);
+
 /* 1D fast-diagonalization tables of the cellwise preconditioner (the 1D set-up
  * of advection_solver_implicit.cc:1020-1062): on the unit interval with the
  * Lagrange basis on the k+1 Gauss points, W^{-1} A1 = V diag(lambda) V^{-1}

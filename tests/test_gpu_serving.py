@@ -1,0 +1,101 @@
+"""Serving loop on the GPU: every solve of a batched mix gives the same
+result as the same request served alone and as the single-mesh LSRK loop,
+the FP64 path matches the oracle, and admission respects the memory budget."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def small_mix(seed=0, n=14):
+    from advection_miniapp_gb300.serving import request_mix
+    return request_mix(n, seed=seed, sizes=(2, 3, 4), degrees=(1, 2, 3, 4, 5, 6), t_range=(0.02, 0.12))
+
+
+def test_mix_equals_alone_and_single_mesh(cuda, adv_lib):
+    from advection_miniapp_gb300.serving import STATE_DONE, Server, run_mix
+    reqs = small_mix()
+    # several degrees and both precisions share the device; step counts are
+    # not multiples of the tick length
+    assert len({(r.degree, r.precision) for r in reqs}) >= 4
+    results, summary, mixed = run_mix(reqs, rate_clock=False, steps_per_tick=4, keep_solutions=True)
+    assert all(results[r.index]["state"] == STATE_DONE for r in reqs)
+    for r in reqs:
+        with Server(keep_solutions=True, steps_per_tick=3) as srv:
+            rid = srv.submit(r)
+            srv.drain()
+            alone = srv.solution(rid, r.n_dofs)
+            res = srv.result(rid)
+        np.testing.assert_array_equal(alone, mixed[r.index])
+        assert res["rel_l2_error"] == results[r.index]["rel_l2_error"]
+        # the single-mesh operator with the same step
+        op = adv_lib.AdvectionOperation(r.config())
+        u, rr, k = (op.initialize_dof_vector() for _ in range(3))
+        op.project_initial(u)
+        op.lsrk_steps(adv_lib.LSRK_5_4, 0.0, res["dt"], res["steps"], u, rr, k)
+        np.testing.assert_array_equal(u.cpu().numpy(), alone)
+        err, nrm = op.l2_error(u, r.t_end)
+        assert abs(err / nrm - res["rel_l2_error"]) <= 1e-12 * max(1.0, err / nrm)
+        assert np.isfinite(res["rel_l2_error"])
+
+
+def test_fp64_request_matches_oracle(cuda, oracle_mod):
+    from advection_miniapp_gb300.serving import Request, Server
+    r = Request(0, 3, 3, (0.6, -0.48, 0.64), (0.25, 0.5, 0.125), 0.05, 0)
+    with Server(keep_solutions=True) as srv:
+        rid = srv.submit(r)
+        srv.drain()
+        u = srv.solution(rid, r.n_dofs)
+        res = srv.result(rid)
+    o = oracle_mod.Oracle(degree=3, n_cells=(3, 3, 3), velocity=r.velocity, ic_params=r.phase)
+    ou, orr, ok = o.project(0.0), o.zeros(), o.zeros()
+    for s in range(res["steps"]):
+        o.lsrk_step(s * res["dt"], res["dt"], ou, orr, ok)
+    assert np.abs(u - ou).max() <= 1e-12 * np.abs(ou).max()
+    err, nrm = o.l2_error(ou, r.t_end)
+    assert abs(res["rel_l2_error"] - err / nrm) <= 1e-10 * err / nrm
+
+
+def test_budget_limits_concurrency(cuda, adv_lib):
+    from advection_miniapp_gb300.serving import Server
+    reqs = small_mix(seed=5, n=10)
+    biggest = max(3 * 8 * r.n_dofs for r in reqs)
+    budget = 2 * biggest
+    with Server(memory_budget_bytes=budget, steps_per_tick=2, keep_solutions=True) as srv:
+        ids = [srv.submit(r) for r in reqs]
+        peak_bytes, peak_running, done = 0, 0, 0
+        while done < len(reqs):
+            done += srv.poll()
+            st = srv.stats()
+            peak_bytes = max(peak_bytes, st["device_bytes"])
+            peak_running = max(peak_running, st["running"])
+        assert peak_bytes <= budget
+        assert 1 <= peak_running < len(reqs)
+        limited = [srv.solution(i, r.n_dofs) for i, r in zip(ids, reqs)]
+    with Server(keep_solutions=True, max_active=3) as srv:
+        ids = [srv.submit(r) for r in reqs]
+        srv.drain()
+        assert srv.stats()["completed"] == len(reqs)
+        capped = [srv.solution(i, r.n_dofs) for i, r in zip(ids, reqs)]
+    for a, b in zip(limited, capped):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_rejected_requests(cuda, adv_lib):
+    from advection_miniapp_gb300.serving import Request, Server
+    r = Request(0, 4, 3, (1.0, 0.0, 0.0), (0.0, 0.0, 0.0), 0.1, 0)
+    with Server(memory_budget_bytes=3 * 8 * r.n_dofs - 1) as srv:
+        with pytest.raises(adv_lib.AdvError):
+            srv.submit(r)
+    with Server() as srv:
+        cfg = r.config()
+        cfg.periodic = 0
+        with pytest.raises(adv_lib.AdvError):
+            srv.submit_config(cfg, 0.1)
+        cfg = r.config()
+        cfg.mesh_type = adv_lib.MESH_DEFORMED
+        with pytest.raises(adv_lib.AdvError):
+            srv.submit_config(cfg, 0.1)
+        with pytest.raises(adv_lib.AdvError):
+            srv.submit_config(r.config(), -1.0)
+        assert srv.stats()["submitted"] == 0
