@@ -99,14 +99,21 @@ class AdvectionOperation:
     """GB300 counterpart of the reference's AdvectionOperation<dim, fe_degree>.
 
     reinit (advection_solver.cc:435-465) happens at construction from an
-    adv_config (or keyword arguments for make_config).
+    adv_config (or keyword arguments for make_config).  With slab=(z_begin,
+    z_end) the operator covers those global z layers of the mesh plus ghost
+    layers (adv_create_slab); the distributed module drives such slabs.
     """
 
-    def __init__(self, config=None, **kw):
+    def __init__(self, config=None, slab=None, **kw):
         self._lib = _lib.load()
         self.config = config if config is not None else make_config(**kw)
         self._h = ctypes.c_void_p()
-        _lib.check(self._lib.adv_create(ctypes.byref(self.config), ctypes.byref(self._h)), "adv_create")
+        self.slab = tuple(slab) if slab is not None else None
+        if self.slab is None:
+            _lib.check(self._lib.adv_create(ctypes.byref(self.config), ctypes.byref(self._h)), "adv_create")
+        else:
+            _lib.check(self._lib.adv_create_slab(ctypes.byref(self.config), int(self.slab[0]), int(self.slab[1]),
+                                                 ctypes.byref(self._h)), "adv_create_slab")
         n = ctypes.c_int64()
         _lib.check(self._lib.adv_n_dofs(self._h, ctypes.byref(n)), "adv_n_dofs")
         self.n_dofs = n.value
@@ -220,7 +227,7 @@ class LowStorageRungeKuttaIntegrator:
         """One time step.  With an AdvectionOperation the whole step runs in the
         library (adv_lsrk_step); any other operator gets the reference's stage
         loop through its perform_stage."""
-        if isinstance(pde_operator, AdvectionOperation):
+        if isinstance(pde_operator, AdvectionOperation) and pde_operator.slab is None:
             pde_operator.lsrk_steps(self.scheme, current_time, time_step, 1, solution, vec_ri, vec_ki,
                                     stream=stream)
             return

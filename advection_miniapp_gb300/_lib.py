@@ -83,6 +83,8 @@ SIGNATURES = {
     "adv_precondition": (_I, [_P, _P, _P, _D, _D, _P]),
     "adv_fgmres": (_I, [_P, _D, _D, _P, _P, _D, _I, ctypes.POINTER(_I), _DP, _P]),
     "adv_bdf2_step": (_I, [_P, _D, _D, _I, _P, _P, _P, _D, ctypes.POINTER(_I), _P]),
+    "adv_create_slab": (_I, [ctypes.POINTER(AdvConfig), _I, _I, ctypes.POINTER(_P)]),
+    "adv_slab_layout": (_I, [ctypes.POINTER(AdvConfig), _I, _I, ctypes.POINTER(_I64)]),
     "adv_server_create": (_I, [_I64, _I, _I, _I, ctypes.POINTER(_P)]),
     "adv_server_destroy": (_I, [_P]),
     "adv_server_submit": (_I, [_P, ctypes.POINTER(AdvConfig), _D, _D, ctypes.POINTER(_I64)]),

@@ -229,7 +229,9 @@ void adv::detail::make_diag(const adv_config &cfg, const adv::Mesh &m, const adv
       g.L[d]  = m.L[d];
       g.h[d]  = m.h[d];
     }
-  g.n_cells     = m.n_cells;
+  g.n_cells     = m.cell_end;
+  g.cell_begin  = m.cell_begin;
+  g.zoff        = m.zoff;
   g.curved      = m.curved;
   g.deformation = h.cfg.deformation;
   g.ex.type     = h.cfg.initial_condition;
@@ -290,8 +292,9 @@ adv::StageArgs base_args(const adv_handle &h, double t)
       A.face_geo[d] = h.d_face_geo[d];
       A.face_x[d]   = h.d_face_x[d];
     }
-  A.n_cells  = m.n_cells;
-  A.periodic = m.periodic;
+  A.n_cells    = m.cell_end;
+  A.cell_begin = m.cell_begin;
+  A.periodic   = m.pmask;
   A.uniform  = m.uniform;
   A.bc_exact = h.cfg.boundary_value == ADV_BOUNDARY_EXACT;
   A.skew     = h.cfg.factor_skew;
@@ -395,13 +398,18 @@ void adv_config_default(adv_config *c)
 
 const char *adv_last_error(void) { return g_last_error.c_str(); }
 
-int adv_create(const adv_config *cfg, adv_handle **out)
+namespace
+{
+// z_end < 0: the whole mesh; else the slab of global z layers [z_begin, z_end)
+int create_handle(const adv_config *cfg, int z_begin, int z_end, adv_handle **out)
 {
   if (!cfg || !out)
     return fail(ADV_ERR_INVALID, "null argument");
   *out = nullptr;
   if (int e = validate(*cfg))
     return e;
+  if (z_end >= 0 && (z_begin < 0 || z_end > cfg->n_cells[2] || z_begin >= z_end))
+    return fail(ADV_ERR_INVALID, "slab range must satisfy 0 <= z_begin < z_end <= n_cells[2]");
   auto *h = new adv_handle();
   h->cfg  = *cfg;
   int rc  = ADV_OK;
@@ -415,7 +423,10 @@ int adv_create(const adv_config *cfg, adv_handle **out)
         }
       if ((rc = ensure_tables(h->device)))
         break;
-      adv::setup_mesh(h->cfg, h->mesh);
+      if (z_end >= 0)
+        adv::setup_slab(h->cfg, z_begin, z_end, h->mesh);
+      else
+        adv::setup_mesh(h->cfg, h->mesh);
       h->tb.init(h->cfg.degree);
       adv::HostGeometry g;
       adv::compute_geometry(h->cfg, h->mesh, h->tb, g);
@@ -466,6 +477,40 @@ int adv_create(const adv_config *cfg, adv_handle **out)
       return rc;
     }
   *out = h;
+  return ADV_OK;
+}
+} // namespace
+
+int adv_create(const adv_config *cfg, adv_handle **out)
+{
+  return create_handle(cfg, 0, -1, out);
+}
+
+int adv_create_slab(const adv_config *cfg, int z_begin, int z_end, adv_handle **out)
+{
+  return create_handle(cfg, z_begin, z_end, out);
+}
+
+int adv_slab_layout(const adv_config *cfg, int z_begin, int z_end, int64_t *out)
+{
+  if (!cfg || !out)
+    return fail(ADV_ERR_INVALID, "null argument");
+  if (int e = validate(*cfg))
+    return e;
+  adv::Mesh m;
+  if (adv::setup_slab(*cfg, z_begin, z_end, m))
+    return fail(ADV_ERR_INVALID, "slab range must satisfy 0 <= z_begin < z_end <= n_cells[2]");
+  const int64_t n3 = (int64_t)m.n * m.n * m.n;
+  out[0] = m.n_dofs;
+  out[1] = m.cell_begin * n3;
+  out[2] = (m.cell_end - m.cell_begin) * n3;
+  out[3] = (int64_t)m.nc[0] * m.nc[1];
+  out[4] = n3;
+  out[5] = m.ghost_lo;
+  out[6] = m.ghost_hi;
+  out[7] = cfg->diffusion != 0.0 ? n3 : (int64_t)m.n * m.n;
+  out[8] = m.nc[2];
+  out[9] = m.zoff;
   return ADV_OK;
 }
 
@@ -649,6 +694,9 @@ int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, 
     return fail(ADV_ERR_ALIASING, "u, r and k must be distinct buffers");
   if (n_steps < 0)
     return fail(ADV_ERR_INVALID, "n_steps must be >= 0");
+  if (h->mesh.slab)
+    return fail(ADV_ERR_INVALID, "a slab needs its ghost layers exchanged before every stage: "
+                                 "call adv_perform_stage per stage");
   if (int e = check_device(h))
     return e;
   std::vector<double> ai, bi;

@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(StageShape<N, T, true, false>::THREADS) batch_
               a.cvf[d] = S.cvf[d], a.Pf[d] = S.Pf[d], a.Mf[d] = S.Mf[d];
             }
           a.n_cells   = (long long)S.n * S.n * S.n;
-          a.periodic  = 1;
+          a.periodic  = 7;
           a.uniform   = 1;
           a.out_scale = 1.0;
           // stage rotation of the three registers (as adv_lsrk_steps)

@@ -24,7 +24,7 @@ constexpr int kMaxN3       = 343;
 __device__ __forceinline__ void cell_origin(const DiagArgs &g, long long c, double lo[3])
 {
   const int ix = (int)(c % g.nc[0]), iy = (int)((c / g.nc[0]) % g.nc[1]),
-            iz = (int)(c / ((long long)g.nc[0] * g.nc[1]));
+            iz = (int)(c / ((long long)g.nc[0] * g.nc[1])) + g.zoff;
   lo[0] = g.lo[0] + ix * g.h[0];
   lo[1] = g.lo[1] + iy * g.h[1];
   lo[2] = g.lo[2] + iz * g.h[2];
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(kDiagThreads) project_kernel(const DiagArgs g,
   extern __shared__ __align__(16) double smem[];
   Layout    L(smem);
   const int n = g.n, nq = n * n * n;
-  for (long long c = blockIdx.x; c < g.n_cells; c += gridDim.x)
+  for (long long c = g.cell_begin + blockIdx.x; c < g.n_cells; c += gridDim.x)
     {
       double lo[3];
       cell_origin(g, c, lo);
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kDiagThreads)
   const int n = g.n, nq = n * n * n;
   double    m = 0.0, e = 0.0, hs = 0.0;
   double   *G[3] = {L.s.A, L.s.B, L.s.By}; // reuse scratch for the three gradients
-  for (long long c = blockIdx.x; c < g.n_cells; c += gridDim.x)
+  for (long long c = g.cell_begin + blockIdx.x; c < g.n_cells; c += gridDim.x)
     {
       double lo[3];
       cell_origin(g, c, lo);
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(kDiagThreads)
   Layout    L(smem);
   const int n = g.n, nq = n * n * n, m = n + 1, m3 = m * m * m;
   double    err = 0.0, nrm = 0.0;
-  for (long long c = blockIdx.x; c < g.n_cells; c += gridDim.x)
+  for (long long c = g.cell_begin + blockIdx.x; c < g.n_cells; c += gridDim.x)
     {
       double lo[3];
       cell_origin(g, c, lo);
@@ -357,7 +357,7 @@ cudaError_t launch_project(const DiagArgs &g, double t, double *dst, cudaStream_
 {
   if (cudaError_t e = opt_in(project_kernel))
     return e;
-  project_kernel<<<diag_max_blocks(g.n_cells), kDiagThreads, kSmemBytes, s>>>(g, t, dst);
+  project_kernel<<<diag_max_blocks(g.n_cells - g.cell_begin), kDiagThreads, kSmemBytes, s>>>(g, t, dst);
   return cudaGetLastError();
 }
 
@@ -366,7 +366,7 @@ cudaError_t launch_mass_energy(const DiagArgs &g, const double *u, double *parti
 {
   if (cudaError_t e = opt_in(mass_energy_kernel))
     return e;
-  *n_blocks = diag_max_blocks(g.n_cells);
+  *n_blocks = diag_max_blocks(g.n_cells - g.cell_begin);
   mass_energy_kernel<<<*n_blocks, kDiagThreads, kSmemBytes, s>>>(g, u, partials);
   return cudaGetLastError();
 }
@@ -376,7 +376,7 @@ cudaError_t launch_l2_error(const DiagArgs &g, const double *u, double t, double
 {
   if (cudaError_t e = opt_in(l2_error_kernel))
     return e;
-  *n_blocks = diag_max_blocks(g.n_cells);
+  *n_blocks = diag_max_blocks(g.n_cells - g.cell_begin);
   l2_error_kernel<<<*n_blocks, kDiagThreads, kSmemBytes, s>>>(g, u, t, partials);
   return cudaGetLastError();
 }

@@ -98,7 +98,7 @@ void cell_support_points(const adv_config &cfg, const Mesh &m, const Tables1D &t
   const int n  = m.n;
   const int ix = int(c % m.nc[0]), iy = int((c / m.nc[0]) % m.nc[1]),
             iz = int(c / ((int64_t)m.nc[0] * m.nc[1]));
-  const double lo[3] = {m.lo[0] + ix * m.h[0], m.lo[1] + iy * m.h[1], m.lo[2] + iz * m.h[2]};
+  const double lo[3] = {m.lo[0] + ix * m.h[0], m.lo[1] + iy * m.h[1], m.lo[2] + (iz + m.zoff) * m.h[2]};
   for (int k = 0; k < n; ++k)
     for (int j = 0; j < n; ++j)
       for (int i = 0; i < n; ++i)
@@ -152,12 +152,40 @@ int setup_mesh(const adv_config &cfg, Mesh &m)
       m.h[d]  = m.L[d] / m.nc[d];
       m.n_cells *= m.nc[d];
     }
+  m.pmask = m.periodic ? 7 : 0;
   for (int d = 0; d < 3; ++d)
     {
       m.npos[d]    = m.periodic ? m.nc[d] : m.nc[d] + 1;
       m.n_faces[d] = (int64_t)m.npos[d] * m.nc[m.t1(d)] * m.nc[m.t2(d)];
     }
-  m.n_dofs = m.n_cells * m.n * m.n * m.n;
+  m.n_dofs     = m.n_cells * m.n * m.n * m.n;
+  m.cell_begin = 0;
+  m.cell_end   = m.n_cells;
+  return 0;
+}
+
+int setup_slab(const adv_config &cfg, int z_begin, int z_end, Mesh &m)
+{
+  setup_mesh(cfg, m);
+  const int nz = cfg.n_cells[2];
+  if (z_begin < 0 || z_end > nz || z_begin >= z_end)
+    return -1;
+  m.slab     = true;
+  m.ghost_lo = m.periodic || z_begin > 0;
+  m.ghost_hi = m.periodic || z_end < nz;
+  m.zoff     = z_begin - (m.ghost_lo ? 1 : 0);
+  m.nc[2]    = (z_end - z_begin) + (m.ghost_lo ? 1 : 0) + (m.ghost_hi ? 1 : 0);
+  m.pmask    = m.periodic ? 3 : 0; // z neighbours come from the ghost layers
+  m.n_cells  = (int64_t)m.nc[0] * m.nc[1] * m.nc[2];
+  for (int d = 0; d < 3; ++d)
+    {
+      m.npos[d]    = ((m.pmask >> d) & 1) ? m.nc[d] : m.nc[d] + 1;
+      m.n_faces[d] = (int64_t)m.npos[d] * m.nc[m.t1(d)] * m.nc[m.t2(d)];
+    }
+  m.n_dofs     = m.n_cells * m.n * m.n * m.n;
+  const int64_t layer = (int64_t)m.nc[0] * m.nc[1];
+  m.cell_begin = m.ghost_lo ? layer : 0;
+  m.cell_end   = m.cell_begin + layer * (z_end - z_begin);
   return 0;
 }
 
@@ -169,10 +197,10 @@ void compute_geometry(const adv_config &cfg, const Mesh &m, const Tables1D &tb, 
   // minimum vertex distance over all cells (setup_dofs, advection_solver.cc:1155-1160)
   double hmin = 1e300;
 #pragma omp parallel for reduction(min : hmin) schedule(static)
-  for (int64_t c = 0; c < m.n_cells; ++c)
+  for (int64_t c = m.cell_begin; c < m.cell_end; ++c)
     {
       const int ix = int(c % m.nc[0]), iy = int((c / m.nc[0]) % m.nc[1]),
-                iz = int(c / ((int64_t)m.nc[0] * m.nc[1]));
+                iz = int(c / ((int64_t)m.nc[0] * m.nc[1])) + m.zoff;
       double v[8][3];
       for (int k = 0; k < 8; ++k)
         {
@@ -274,14 +302,15 @@ void compute_geometry(const adv_config &cfg, const Mesh &m, const Tables1D &tb, 
             const int p  = int(f % m.npos[d]);
             const int j1 = int((f / m.npos[d]) % m.nc[t1]);
             const int j2 = int(f / ((int64_t)m.npos[d] * m.nc[t1]));
-            const bool boundary = !m.periodic && (p == 0 || p == m.nc[d]);
+            const bool wrap     = (m.pmask >> d) & 1;
+            const bool boundary = !wrap && (p == 0 || p == m.nc[d]);
             if (!need_coef && !boundary)
               continue;
             // the cell on the low side (or the only cell of a boundary face)
             int ijk[3];
             ijk[t1] = j1, ijk[t2] = j2;
             int side;
-            if (m.periodic)
+            if (wrap)
               ijk[d] = (p - 1 + m.nc[d]) % m.nc[d], side = 1;
             else if (p == 0)
               ijk[d] = 0, side = 0;

@@ -31,6 +31,14 @@ struct Mesh
   bool    uniform  = true; // affine + constant velocity: geometry is a set of constants
   int     npos[3] = {};    // face positions per direction (nc or nc + 1)
   int64_t n_faces[3] = {}; // faces per direction = npos * product of tangential counts
+  // slab of a z-partitioned mesh: the local cells are the owned layers plus
+  // one ghost layer on each side that has a neighbouring slab (or wraps
+  // periodically); local layer 0 is global layer zoff.  h stays global.
+  int     pmask      = 7;  // bit d: periodic wrap along d inside the local cells
+  int     zoff       = 0;
+  int64_t cell_begin = 0, cell_end = 0; // owned local cells
+  bool    slab       = false;
+  bool    ghost_lo = false, ghost_hi = false;
 
   int t1(int d) const { return d == 0 ? 1 : 0; }
   int t2(int d) const { return d == 2 ? 1 : 2; }
@@ -65,5 +73,7 @@ void deform_point(const adv_config &cfg, const double L[3], const double x[3], d
 void velocity_field(const adv_config &cfg, const double x[3], double b[3]);
 
 int  setup_mesh(const adv_config &cfg, Mesh &m);
+// local mesh of the slab of global z layers [z_begin, z_end) with its ghost layers
+int  setup_slab(const adv_config &cfg, int z_begin, int z_end, Mesh &m);
 void compute_geometry(const adv_config &cfg, const Mesh &m, const Tables1D &tb, HostGeometry &g);
 } // namespace adv

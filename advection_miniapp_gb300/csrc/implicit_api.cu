@@ -122,6 +122,9 @@ int adv_solver_create(adv_handle *h, int restart, int precond_precision, adv_sol
     return fail(ADV_ERR_INVALID, "the implicit solver needs an FP64 operator handle (residuals are FP64)");
   if (h->cfg.diffusion != 0.0)
     return fail(ADV_ERR_INVALID, "the implicit solver covers advection without diffusion");
+  if (h->mesh.slab)
+    return fail(ADV_ERR_INVALID, "the implicit solver runs on whole meshes (its inner products are not reduced "
+                                 "across slabs)");
   if (!h->mesh.periodic && h->cfg.boundary_value != ADV_BOUNDARY_ZERO)
     return fail(ADV_ERR_INVALID, "the implicit solver needs periodic meshes or zero Dirichlet data (a linear operator)");
   if (int e = adv::detail::check_device(h))

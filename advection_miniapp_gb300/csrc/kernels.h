@@ -31,8 +31,9 @@ struct StageArgs
   int           swap_pm;  // velocity time factor < 0: exchange the upwind coefficients
   int           nc[3];
   int           npos[3];
-  long long     n_cells;
-  int           periodic;
+  long long     n_cells;    // end of the processed cells (local index)
+  long long     cell_begin; // first processed cell (a slab skips its lower ghost layer)
+  int           periodic;   // bit d: wrap around along d
   int           uniform;  // affine mesh with constant velocity
   int           bc_exact; // Dirichlet data from the exact solution (else zero)
   int           pad0;
@@ -80,7 +81,10 @@ struct DiagArgs
 {
   int           n;
   int           nc[3];
-  long long     n_cells;
+  long long     n_cells;    // end of the owned cells (local index)
+  long long     cell_begin; // first owned cell
+  int           zoff;       // global z index of local cell layer 0
+  int           pad1;
   double        lo[3], L[3], h[3];
   int           curved;
   int           pad0;

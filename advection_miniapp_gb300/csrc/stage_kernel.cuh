@@ -318,12 +318,13 @@ __device__ __forceinline__ void stage_cta(const StageArgs &A, const long long ce
       const int j2  = d == 2 ? iy : iz;
       const int n1  = d == 0 ? ny : nx;
       const int npd = d == 0 ? A.npos[0] : d == 1 ? A.npos[1] : A.npos[2];
-      int       pos = id + s;
-      if (A.periodic && pos == nd)
+      const bool wrap = (A.periodic >> d) & 1;
+      int        pos  = id + s;
+      if (wrap && pos == nd)
         pos = 0;
       s_face[i] = pos + npd * (j1 + n1 * j2);
       int nb    = id + (s ? 1 : -1);
-      if (A.periodic)
+      if (wrap)
         nb = (nb + nd) % nd;
       if (nb < 0 || nb >= nd)
         s_nbr[i] = -1;
@@ -664,7 +665,7 @@ __global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS)
   stage_kernel(const StageArgs A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_cta<N, T, UNI, VISC>(A, (long long)blockIdx.x * StageShape<N, T, UNI, VISC>::C, smem_raw);
+  stage_cta<N, T, UNI, VISC>(A, A.cell_begin + (long long)blockIdx.x * StageShape<N, T, UNI, VISC>::C, smem_raw);
 }
 
 template <int N, typename T, bool UNI, bool VISC>
@@ -686,7 +687,7 @@ cudaError_t launch_stage_t(const StageArgs &args, cudaStream_t stream)
       if (dev < 64)
         configured |= 1ull << dev;
     }
-  const long long blocks = (args.n_cells + SH::C - 1) / SH::C;
+  const long long blocks = (args.n_cells - args.cell_begin + SH::C - 1) / SH::C;
   stage_kernel<N, T, UNI, VISC><<<(unsigned)blocks, SH::THREADS, SH::SMEM, stream>>>(args);
   return cudaGetLastError();
 }

@@ -90,6 +90,25 @@ void adv_config_default(adv_config *cfg);
 /* AdvectionOperation::reinit (advection_solver.cc:435-465): builds the mesh,
  * the 1D tables and the geometry on the current device and uploads them. */
 int adv_create(const adv_config *cfg, adv_handle **out);
+
+/* Slab of a mesh partitioned along z, one per rank (the reference distributes
+ * cells with parallel::distributed::Triangulation and exchanges face values
+ * in MatrixFree::loop with DataAccessOnFaces::values, advection_solver.cc:
+ * 678-679).  The handle owns global z layers [z_begin, z_end) and holds one
+ * ghost layer of cells below and above wherever a neighbouring slab exists
+ * (always on periodic meshes).  Its vectors are local: the ghost layers, then
+ * the owned layers, cell-major with x fastest, n^3 nodal values per cell with
+ * the z index slowest.  The caller fills the ghost layers of the source vector
+ * before every adv_apply / adv_perform_stage / adv_vmult (only each ghost
+ * cell's face layer next to the slab, or whole cells with diffusion);
+ * diagnostics cover the owned cells and return per-slab sums to be added
+ * across ranks.  Fused step loops and the implicit solver reject slabs. */
+int adv_create_slab(const adv_config *cfg, int z_begin, int z_end, adv_handle **out);
+/* Host-only layout of that slab: out[10] = {local dofs (with ghosts), first
+ * owned dof, owned dofs, cells per z layer, dofs per cell, ghost layer below
+ * (0/1), ghost layer above (0/1), values per cell exchanged (n^2 face layer,
+ * n^3 with diffusion), local z layers, global z index of local layer 0}. */
+int adv_slab_layout(const adv_config *cfg, int z_begin, int z_end, int64_t *out);
 /* AdvectionOperation destructor (advection_solver.cc:349-372): frees device data. */
 int adv_destroy(adv_handle *h);
 const char *adv_last_error(void);
