@@ -92,13 +92,12 @@ double det_inverse(const double *J, double *Ji)
   return det;
 }
 
-void cell_support_points(const adv_config &cfg, const Mesh &m, const Tables1D &tb, int64_t c,
+// support points of the cell with global indices (ix, iy, iz)
+void cell_support_points(const adv_config &cfg, const Mesh &m, const Tables1D &tb, int ix, int iy, int iz,
                          double *X)
 {
-  const int n  = m.n;
-  const int ix = int(c % m.nc[0]), iy = int((c / m.nc[0]) % m.nc[1]),
-            iz = int(c / ((int64_t)m.nc[0] * m.nc[1]));
-  const double lo[3] = {m.lo[0] + ix * m.h[0], m.lo[1] + iy * m.h[1], m.lo[2] + (iz + m.zoff) * m.h[2]};
+  const int    n     = m.n;
+  const double lo[3] = {m.lo[0] + ix * m.h[0], m.lo[1] + iy * m.h[1], m.lo[2] + iz * m.h[2]};
   for (int k = 0; k < n; ++k)
     for (int j = 0; j < n; ++j)
       for (int i = 0; i < n; ++i)
@@ -111,6 +110,13 @@ void cell_support_points(const adv_config &cfg, const Mesh &m, const Tables1D &t
           else
             y[0] = p[0], y[1] = p[1], y[2] = p[2];
         }
+}
+
+// support points of local cell c
+void cell_support_points(const adv_config &cfg, const Mesh &m, const Tables1D &tb, int64_t c, double *X)
+{
+  cell_support_points(cfg, m, tb, int(c % m.nc[0]), int((c / m.nc[0]) % m.nc[1]),
+                      int(c / ((int64_t)m.nc[0] * m.nc[1])) + m.zoff, X);
 }
 } // namespace
 
@@ -161,6 +167,7 @@ int setup_mesh(const adv_config &cfg, Mesh &m)
   m.n_dofs     = m.n_cells * m.n * m.n * m.n;
   m.cell_begin = 0;
   m.cell_end   = m.n_cells;
+  m.gnz        = m.nc[2];
   return 0;
 }
 
@@ -316,8 +323,21 @@ void compute_geometry(const adv_config &cfg, const Mesh &m, const Tables1D &tb, 
               ijk[d] = 0, side = 0;
             else
               ijk[d] = p - 1, side = 1;
-            const int64_t c = ijk[0] + (int64_t)m.nc[0] * (ijk[1] + (int64_t)m.nc[1] * ijk[2]);
-            cell_support_points(cfg, m, tb, c, X.data());
+            // global z index of that cell: a slab takes the cell the whole
+            // mesh takes (across a periodic seam the wrapped one), so that
+            // both compute bit-identical face data
+            int gz = ijk[2] + m.zoff;
+            if (d == 2 && m.slab)
+              {
+                const int pg = p + m.zoff;
+                if (m.periodic)
+                  gz = (pg - 1 + m.gnz) % m.gnz, side = 1;
+                else if (pg == 0)
+                  gz = 0, side = 0;
+                else
+                  gz = pg - 1, side = 1;
+              }
+            cell_support_points(cfg, m, tb, ijk[0], ijk[1], gz, X.data());
             // 1D tables: normal direction at xi_d = side, tangential at the Gauss points
             int np[3];
             for (int e = 0; e < 3; ++e)

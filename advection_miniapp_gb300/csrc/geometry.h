@@ -36,6 +36,7 @@ struct Mesh
   // periodically); local layer 0 is global layer zoff.  h stays global.
   int     pmask      = 7;  // bit d: periodic wrap along d inside the local cells
   int     zoff       = 0;
+  int     gnz        = 0;  // cells along z of the whole mesh
   int64_t cell_begin = 0, cell_end = 0; // owned local cells
   bool    slab       = false;
   bool    ghost_lo = false, ghost_hi = false;
