@@ -12,13 +12,14 @@ per element like the reference's summary (advection_solver.cc:1302-1311).
 """
 import argparse
 import json
+import math
 import time
 
 import torch
 
 from . import (AdvectionOperation, IC_BLOB, IC_SINE_GAUSS, IC_WAVE, LSRK_3_3, LSRK_5_4, LSRK_7_4, LSRK_9_5,
                LowStorageRungeKuttaIntegrator, MESH_CARTESIAN, MESH_DEFORMED, PRECISION_FP32_OPERATOR,
-               PRECISION_FP64, make_config)
+               PRECISION_FP64, make_config, workload_config)
 
 SCHEMES = {"3_3": LSRK_3_3, "5_4": LSRK_5_4, "7_4": LSRK_7_4, "9_5": LSRK_9_5}
 ICS = {"sine-gauss": IC_SINE_GAUSS, "blob": IC_BLOB, "wave": IC_WAVE}
@@ -26,6 +27,10 @@ ICS = {"sine-gauss": IC_SINE_GAUSS, "blob": IC_BLOB, "wave": IC_WAVE}
 
 def parse(argv=None):
     p = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    p.add_argument("--workload", default=None,
+                   help="a named workload (workload_config) instead of the mesh/degree/velocity options")
+    p.add_argument("--t-end", type=float, default=None,
+                   help="run to this time (steps = ceil(t_end / dt), dt rounded to t_end / steps)")
     p.add_argument("--mesh", choices=["cartesian", "deformed"], default="cartesian")
     p.add_argument("--cells", type=int, default=8, help="cells per direction")
     p.add_argument("--degree", type=int, default=3)
@@ -40,6 +45,8 @@ def parse(argv=None):
     p.add_argument("--skew", type=float, default=0.0)
     p.add_argument("--output-every", type=int, default=0, help="0: only at the start and the end")
     p.add_argument("--json", action="store_true", help="print one JSON summary line")
+    p.add_argument("--compare-fp64", action="store_true",
+                   help="FP32 operator: rerun with the FP64 operator and report both errors and the difference")
     p.add_argument("--implicit", action="store_true",
                    help="BDF2 steps with FGMRES and the block-Jacobi FDM preconditioner instead of LSRK")
     p.add_argument("--restart", type=int, default=30, help="FGMRES restart length (implicit)")
@@ -89,12 +96,15 @@ def run_implicit(args, op):
 
 def main(argv=None):
     args = parse(argv)
-    cfg = make_config(degree=args.degree, n_cells=(args.cells,) * 3,
-                      mesh_type=MESH_DEFORMED if args.mesh == "deformed" else MESH_CARTESIAN,
-                      deformation=args.deformation if args.mesh == "deformed" else 0.0,
-                      velocity=tuple(args.velocity), initial_condition=ICS[args.initial_condition],
-                      flux_alpha=args.flux_alpha, factor_skew=args.skew,
-                      precision=PRECISION_FP64 if args.precision == "fp64" else PRECISION_FP32_OPERATOR)
+    precision = PRECISION_FP64 if args.precision == "fp64" else PRECISION_FP32_OPERATOR
+    if args.workload:
+        cfg = workload_config(args.workload, precision=precision)
+    else:
+        cfg = make_config(degree=args.degree, n_cells=(args.cells,) * 3,
+                          mesh_type=MESH_DEFORMED if args.mesh == "deformed" else MESH_CARTESIAN,
+                          deformation=args.deformation if args.mesh == "deformed" else 0.0,
+                          velocity=tuple(args.velocity), initial_condition=ICS[args.initial_condition],
+                          flux_alpha=args.flux_alpha, factor_skew=args.skew, precision=precision)
     op = AdvectionOperation(cfg)
     if args.implicit:
         res = run_implicit(args, op)
@@ -106,6 +116,10 @@ def main(argv=None):
         return
     integ = LowStorageRungeKuttaIntegrator(SCHEMES[args.scheme])
     dt = op.time_step(args.courant)
+    if args.t_end is not None:
+        # rounding of setup_dofs (advection_solver.cc:1161-1167)
+        args.steps = max(1, math.ceil(args.t_end / dt - 1e-12))
+        dt = args.t_end / args.steps
     if not args.json:
         print(f"   Number of elements:            {op.n_cells}")
         print(f"   Polynomial degree:             {op.degree}")
@@ -144,9 +158,25 @@ def main(argv=None):
             rel, me = output(step, t)
     per_step = wall / max(args.steps, 1)
     stage_rate = op.n_dofs * integ.n_stages() * args.steps / wall / 1e9 if wall > 0 else 0.0
+    res = {"workload": args.workload, "precision": args.precision, "n_dofs": op.n_dofs, "steps": args.steps,
+           "dt": dt, "t_end": t, "rel_l2_error": rel, "mass_energy": list(me), "s_per_step": per_step,
+           "gdofs_per_stage": stage_rate}
+    if args.compare_fp64 and precision != PRECISION_FP64:
+        cfg.precision = PRECISION_FP64
+        op64 = AdvectionOperation(cfg)
+        u64, r64, k64 = (op64.initialize_dof_vector() for _ in range(3))
+        op64.project_initial(u64)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        op64.lsrk_steps(integ.scheme, 0.0, dt, args.steps, u64, r64, k64)
+        torch.cuda.synchronize()
+        wall64 = time.perf_counter() - t0
+        e64, n64 = op64.l2_error(u64, t)
+        res["fp64"] = {"rel_l2_error": e64 / n64, "gdofs_per_stage": op.n_dofs * integ.n_stages() * args.steps
+                       / wall64 / 1e9, "max_rel_difference": float((u - u64).abs().max() / u64.abs().max()),
+                       "error_ratio_fp32_over_fp64": rel / (e64 / n64)}
     if args.json:
-        print(json.dumps({"n_dofs": op.n_dofs, "steps": args.steps, "dt": dt, "t_end": t, "rel_l2_error": rel,
-                          "mass_energy": list(me), "s_per_step": per_step, "gdofs_per_stage": stage_rate}))
+        print(json.dumps(res))
     else:
         print(f"\n   Performed {args.steps} time steps.")
         print(f"   Average wall clock time per time step: {per_step:.4g}s, time per element: "
