@@ -812,9 +812,24 @@ int adv_time_step(adv_handle *h, double courant, double *dt)
     return fail(ADV_ERR_INVALID, "null argument");
   const double *a    = h->cfg.velocity;
   const double  anrm = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
-  if (!(anrm > 0.0))
+  const double  nu   = h->cfg.diffusion;
+  if (!(anrm > 0.0) && !(nu > 0.0))
     return fail(ADV_ERR_INVALID, "zero velocity");
-  *dt = courant * h->h_min / anrm / std::pow(std::max(1, h->cfg.degree), 1.5);
+  // advective limit of setup_dofs (advection_solver.cc:1155-1165)
+  const double dt_a = courant * h->h_min / anrm / std::pow(std::max(1, h->cfg.degree), 1.5);
+  // explicit SIPG: the spectral radius of M^{-1} A_diff is at most about
+  // 7 nu (k+1)^4 / h^2 with the penalty (k+1)^2 / h (power iteration, k = 1..6),
+  // LSRK(5,4) is stable on the negative real axis down to -4.8; the diffusive
+  // limit 0.3 h^2 / (nu (k+1)^4) keeps its eigenvalues within -2.1 and is
+  // combined harmonically with the advective one
+  const double k1 = h->cfg.degree + 1.0;
+  if (!(nu > 0.0))
+    *dt = dt_a;
+  else
+    {
+      const double dt_d = 0.3 * h->h_min * h->h_min / (nu * k1 * k1 * k1 * k1);
+      *dt               = anrm > 0.0 ? 1.0 / (1.0 / dt_a + 1.0 / dt_d) : dt_d;
+    }
   return ADV_OK;
 }
 

@@ -1597,10 +1597,21 @@ double oracle_min_vertex_distance(oracle_op *h)
 // FINAL_TIME / ceil(FINAL_TIME / dt))
 double oracle_time_step(oracle_op *h, double courant)
 {
-  const double *a    = h->op.ph.cfg.velocity;
-  const double  anrm = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
-  const double  k    = std::max(1, h->op.ph.cfg.degree);
-  return courant * oracle_min_vertex_distance(h) / anrm / std::pow(k, 1.5);
+  // advective limit: setup_dofs, advection_solver.cc:1155-1165
+  const double *a     = h->op.ph.cfg.velocity;
+  const double  anrm  = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+  const double  k     = std::max(1, h->op.ph.cfg.degree);
+  const double  hmin  = oracle_min_vertex_distance(h);
+  const double  dt_a  = courant * hmin / anrm / std::pow(k, 1.5);
+  // with SIPG diffusion nu, the explicit limit 0.3 h^2 / (nu (k+1)^4) is
+  // combined harmonically (a builder rule: the reference integrates its
+  // advection-diffusion problem implicitly, advection_diffusion_solver.cc:1463)
+  const double nu = h->op.ph.cfg.diffusion;
+  const double k1 = h->op.ph.cfg.degree + 1.0;
+  if (!(nu > 0.0))
+    return dt_a;
+  const double dt_d = 0.3 * hmin * hmin / (nu * k1 * k1 * k1 * k1);
+  return anrm > 0.0 ? 1.0 / (1.0 / dt_a + 1.0 / dt_d) : dt_d;
 }
 
 int oracle_support_points(oracle_op *h, double *xyz)

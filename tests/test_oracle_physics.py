@@ -154,3 +154,26 @@ def test_time_step_rule(oracle_mod):
     expected = 0.5 * 0.125 / np.sqrt(1.0 + 0.15 ** 2 + 0.05 ** 2) / 3 ** 1.5
     assert abs(o.time_step(0.5) - expected) < 1e-15
     assert abs(expected - 0.0118805) < 1e-6
+
+
+def test_time_step_with_diffusion_is_stable(oracle_mod):
+    """The diffusive limit: 4^3 cells of degree 5 with nu = 8e-3 have the
+    ratio of diffusive to advective stiffness (proportional to nu / h) of the
+    32^3 advection-diffusion workload with nu = 1e-3; with the combined rule
+    the energy decays over 60 steps (the advective rule alone reaches 1e29
+    within 20 steps)."""
+    cfg = dict(degree=5, n_cells=(4, 4, 4), periodic=0, velocity_type=1, velocity=(1.0, 1.0, 0.3),
+               velocity_period=0.5, diffusion=8e-3, initial_condition=1, ic_params=(0.3, 0.5, 0.5, 0.2),
+               boundary_value=0)
+    o = oracle_mod.Oracle(**cfg)
+    h, k1, nu = 0.25, 6.0, 8e-3
+    dt_a = 0.5 * h / np.sqrt(2.09) / 5 ** 1.5
+    dt_d = 0.3 * h * h / (nu * k1 ** 4)
+    dt = o.time_step(0.5)
+    assert abs(dt - 1.0 / (1.0 / dt_a + 1.0 / dt_d)) <= 1e-15 * dt
+    u = o.project(0.0)
+    r, k = o.zeros(), o.zeros()
+    e0 = o.mass_energy(u)[1]
+    for s in range(60):
+        o.lsrk_step(s * dt, dt, u, r, k)
+    assert np.isfinite(u).all() and o.mass_energy(u)[1] < e0
