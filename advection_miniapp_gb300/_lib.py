@@ -19,6 +19,7 @@ IC_SINE_GAUSS, IC_BLOB, IC_WAVE = 0, 1, 2
 BOUNDARY_ZERO, BOUNDARY_EXACT = 0, 1
 PRECISION_FP64, PRECISION_FP32_OPERATOR = 0, 1
 LSRK_3_3, LSRK_5_4, LSRK_7_4, LSRK_9_5 = 0, 1, 2, 3
+FORM_AUTO, FORM_NODAL, FORM_COLLOCATION = 0, 1, 2
 
 
 class AdvConfig(ctypes.Structure):
@@ -43,7 +44,8 @@ class AdvConfig(ctypes.Structure):
         ("reserved0", ctypes.c_int32),
         ("ic_params", ctypes.c_double * 8),
         ("precision", ctypes.c_int32),
-        ("reserved1", ctypes.c_int32 * 7),
+        ("fused_form", ctypes.c_int32),
+        ("reserved1", ctypes.c_int32 * 6),
     ]
 
 

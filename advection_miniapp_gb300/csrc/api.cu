@@ -150,6 +150,8 @@ int ensure_tables(int device)
   ADV_CUDA(adv::upload_tables_diag(td, tf));
   ADV_CUDA(adv::upload_tables_implicit(td, tf));
   ADV_CUDA(adv::upload_tables_batch(td, tf));
+  ADV_CUDA(adv::upload_tables_gauss64(td, tf));
+  ADV_CUDA(adv::upload_tables_gauss32(td, tf));
   g_tables_uploaded[device] = true;
   return ADV_OK;
 }
@@ -158,6 +160,8 @@ int validate(const adv_config &c)
 {
   if (c.degree < 1 || c.degree > 6)
     return fail(ADV_ERR_INVALID, "degree must be in 1..6");
+  if (c.fused_form < ADV_FORM_AUTO || c.fused_form > ADV_FORM_COLLOCATION)
+    return fail(ADV_ERR_INVALID, "unknown fused_form");
   for (int d = 0; d < 3; ++d)
     {
       if (c.n_cells[d] < 1)
@@ -331,12 +335,27 @@ adv::StageArgs base_args(const adv_handle &h, double t)
 
 int launch(adv_handle *h, const adv::StageArgs &A, cudaStream_t s)
 {
-  cudaError_t e = h->cfg.precision == ADV_PRECISION_FP64 ? adv::launch_stage_fp64(h->mesh.n, A, s)
-                                                           : adv::launch_stage_fp32(h->mesh.n, A, s);
+  const bool  fp64 = h->cfg.precision == ADV_PRECISION_FP64;
+  cudaError_t e    = A.gauss ? (fp64 ? adv::launch_stage_gauss_fp64(h->mesh.n, A, s)
+                                     : adv::launch_stage_gauss_fp32(h->mesh.n, A, s))
+                             : (fp64 ? adv::launch_stage_fp64(h->mesh.n, A, s)
+                                     : adv::launch_stage_fp32(h->mesh.n, A, s));
   if (e != cudaSuccess)
     return cuda_fail(e, "stage kernel launch");
   ++h->launches;
   return ADV_OK;
+}
+
+// Basis of the fused step loop: the collocation form wherever it is the
+// faster one (measured: the FP64 operator, whose stages are bound by the
+// FP64 pipe and lose about 40 % of their instructions)
+bool use_collocation(const adv_handle &h)
+{
+  if (h.cfg.fused_form == ADV_FORM_NODAL)
+    return false;
+  if (h.cfg.fused_form == ADV_FORM_COLLOCATION)
+    return true;
+  return h.cfg.precision == ADV_PRECISION_FP64;
 }
 
 int ensure_scratch(adv_handle *h, int i)
@@ -704,6 +723,16 @@ int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, 
     return fail(ADV_ERR_INVALID, "unknown LSRK scheme");
   cudaStream_t s  = (cudaStream_t)stream;
   const int    ns = (int)bi.size();
+  if (ns == 1)
+    return fail(ADV_ERR_INVALID, "one-stage schemes are not supported");
+  // collocation form: the solution moves to the Gauss-point values for the
+  // steps and back afterwards (r and k are scratch either way)
+  const bool gauss = n_steps > 0 && use_collocation(*h);
+  if (gauss)
+    {
+      ADV_CUDA(adv::launch_basis_change(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, true, s));
+      ++h->launches;
+    }
   for (int step = 0; step < n_steps; ++step)
     {
       const double t0 = t + step * dt;
@@ -719,6 +748,7 @@ int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, 
           adv::StageArgs A   = base_args(*h, ts);
           const double   fac = A.out_scale;
           const bool     last = st == ns - 1;
+          A.gauss             = gauss;
           A.b                 = bi[st] * dt * fac;
           A.a                 = last ? 0.0 : ai[st] * dt * fac;
           A.mode              = last ? adv::kModeLastStage : adv::kModeStage;
@@ -736,14 +766,14 @@ int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, 
               double *rout = (st % 2 == 0) ? r : k;
               A.r_in = rin, A.u_in = u, A.u_out = u, A.r_out = last ? nullptr : rout;
             }
-          if (ns == 1)
-            {
-              // a one-stage scheme would leave the solution in K; not a scheme of the reference
-              return fail(ADV_ERR_INVALID, "one-stage schemes are not supported");
-            }
           if (int e = launch(h, A, s))
             return e;
         }
+    }
+  if (gauss)
+    {
+      ADV_CUDA(adv::launch_basis_change(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, false, s));
+      ++h->launches;
     }
   return ADV_OK;
 }

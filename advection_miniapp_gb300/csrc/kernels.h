@@ -36,7 +36,7 @@ struct StageArgs
   int           periodic;   // bit d: wrap around along d
   int           uniform;  // affine mesh with constant velocity
   int           bc_exact; // Dirichlet data from the exact solution (else zero)
-  int           pad0;
+  int           gauss;    // vectors hold values at the Gauss points (collocation basis)
   double        cv[3], P[3], M[3]; // uniform case: a_d / h_d and face coefficients
   double        skew;
   float         cvf[3], Pf[3], Mf[3], skewf; // the same in binary32 for the FP32 operator
@@ -62,6 +62,21 @@ struct StageArgs
 
 // precision: 0 = FP64, 1 = FP32 operator
 cudaError_t launch_stage(int n, int precision, const StageArgs &args, cudaStream_t stream);
+
+// Collocation form of the stage (args.gauss != 0): r_in, u_in and the outputs
+// hold the values at the (k+1)^3 Gauss points of every cell, the nodal basis
+// of the Lagrange polynomials on those points.  The operator is the same
+// polynomial map as the Gauss-Lobatto nodal form without its interpolation
+// and inverse-mass sweeps.  Modes: apply, stage, last stage.
+cudaError_t launch_stage_gauss_fp64(int n, const StageArgs &args, cudaStream_t stream);
+cudaError_t launch_stage_gauss_fp32(int n, const StageArgs &args, cudaStream_t stream);
+cudaError_t upload_tables_gauss64(const DevTables<double> *d, const DevTables<float> *f);
+cudaError_t upload_tables_gauss32(const DevTables<double> *d, const DevTables<float> *f);
+// In-place change of basis of the cells [cell_begin, cell_end) of u:
+// to_gauss: Gauss-Lobatto nodal values -> values at the Gauss points (S x S x S);
+// otherwise the inverse (S^-1 x S^-1 x S^-1).
+cudaError_t launch_basis_change(int n, double *u, long long cell_begin, long long cell_end, bool to_gauss,
+                                cudaStream_t stream);
 // cells processed per CTA by the stage kernel (for launch accounting)
 int stage_cells_per_block(int n, int precision);
 

@@ -1,0 +1,249 @@
+// Fused DG advection stage in collocation form for sm_103a.
+//
+// The vectors hold, per cell, the values at the (k+1)^3 Gauss points: the
+// nodal basis of the Lagrange polynomials on the Gauss points spans the same
+// space as the reference's FE_DGQ basis on Gauss-Lobatto nodes, and the two
+// coefficient vectors are related by U = (S x S x S) u.  In this basis the
+// stage of the nodal kernel (stage_kernel.cuh) loses its interpolation and
+// inverse-mass sweeps:
+//   Z = idet * [ sum_d Dw_d (vt_d . U) + sum_faces lw(s) phi ]
+// is already the Gauss-point representation of k = M^{-1} L(u)
+// (advection_solver.cc:469-657), because M^{-1} = S^{-1} diag(1/JxW) S^{-T}
+// and the S^{-T} cancels against the transposed interpolation of the
+// integration.  Face values of a neighbour are contractions of its pencil
+// through the face point with its Lagrange basis at the shared face, so each
+// cell reads whole neighbour cells (n^3 values, from L2) instead of their
+// Gauss-Lobatto face layers.  Per cell and stage at degree 4 this removes 6 of
+// the 9 n^4 sweeps and replaces the 2D interpolation of the neighbour layers
+// by n^3 contractions: about 4.9k instead of 8.4k FP64 instructions.
+//
+// The fused LSRK loop changes the basis of the solution once on entry and
+// once on exit (launch_basis_change); the stages in between run here.
+#pragma once
+
+#include "stage_kernel.cuh"
+
+namespace adv
+{
+template <int N, typename T, bool UNI, bool VISC>
+__device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long long cell0,
+                                                unsigned char *smem_raw)
+{
+  using SH         = StageShape<N, T, UNI, VISC>;
+  constexpr int C  = SH::C;
+  constexpr int NQ = SH::NQ;
+  constexpr int NF = SH::NF;
+  constexpr int NT = SH::THREADS;
+  T   *Ub     = reinterpret_cast<T *>(smem_raw); // [C][NQ] Gauss-point values of r_in
+  T   *Qb     = Ub + C * NQ;                     // [C][NQ] x and y contributions to Z
+  T   *Nb     = Qb + C * NQ;                     // [C][6][NF] neighbour values at the face points
+  T   *Gb     = Nb + C * 6 * NF;                 // field: [C][4][NQ] cell geometry
+  T   *Fb     = Gb + (UNI ? 0 : C * 4 * NQ);     // field: [C][6][2][NF] face coefficients
+  T   *Nd     = Fb + (UNI ? 0 : C * 12 * NF);    // viscous: [C][6][NF] neighbour normal derivatives
+  int *s_nbr  = reinterpret_cast<int *>(Nd + (VISC ? C * 6 * NF : 0));
+  int *s_face = s_nbr + C * 6;
+
+  const DevTables<T> &tb    = tab<T>(N);
+  const int           tid   = threadIdx.x;
+  const int           ncell = (int)min((long long)C, A.n_cells - cell0);
+
+  cell_neighbours(A, cell0, ncell, s_nbr, s_face, tid, NT);
+  __syncthreads();
+  if (!UNI)
+    geometry_async<N, T>(A, cell0, ncell, s_face, Gb, Fb, tid, NT);
+
+  // ---- phase 1: own values (one contiguous range of the CTA's cells) and
+  //      the neighbours' values at the face points
+  {
+    const double *src = A.r_in + cell0 * NQ;
+    for (int i = tid; i < ncell * NQ; i += NT)
+      Ub[i] = from_double<T>(__ldg(src + i));
+  }
+  for (int w = tid; w < ncell * 6 * NF; w += NT)
+    {
+      const int cf = w / NF, fq = w % NF;
+      const int j = cf % 6, d = j >> 1;
+      const int nb = s_nbr[cf];
+      if (nb >= 0)
+        {
+          // pencil of the neighbour along d through face point fq, contracted
+          // with its basis at the shared face: xi_d = 1 for the neighbour
+          // below (low face, j even), xi_d = 0 for the one above
+          const T      *l  = (j & 1) ? tb.l0 : tb.l1;
+          const int     sd = d == 0 ? 1 : d == 1 ? N : NF;
+          const double *g  = A.r_in + (long long)nb * NQ + idx3<N>(d, 0, fq % N, fq / N);
+          T             v[N];
+#pragma unroll
+          for (int a = 0; a < N; ++a)
+            v[a] = from_double<T>(__ldg(g + a * sd));
+          T s = l[0] * v[0];
+#pragma unroll
+          for (int a = 1; a < N; ++a)
+            s = fma(l[a], v[a], s);
+          Nb[cf * NF + fq] = s;
+          if (VISC)
+            {
+              const T *ld = (j & 1) ? tb.ld0 : tb.ld1;
+              T        ds = ld[0] * v[0];
+#pragma unroll
+              for (int a = 1; a < N; ++a)
+                ds = fma(ld[a], v[a], ds);
+              Nd[cf * NF + fq] = ds;
+            }
+        }
+      else
+        {
+          double g = 0.0;
+          if (A.bc_exact)
+            {
+              const double *fx = d == 0 ? A.face_x[0] : d == 1 ? A.face_x[1] : A.face_x[2];
+              const double *x  = fx + ((size_t)s_face[cf] * NF + fq) * 3;
+              g                = exact_value(A.ex, x[0], x[1], x[2], A.t);
+            }
+          Nb[cf * NF + fq] = from_double<T>(g);
+        }
+    }
+  if (!UNI)
+    __pipeline_wait_prior(0);
+  __syncthreads();
+
+  // ---- phase 2: x-direction terms
+  for (int w = tid; w < ncell * NF; w += NT)
+    {
+      const int cl = w / NF, r = w % NF;
+      const T  *p  = Ub + cl * NQ + N * r;
+      T         U[N], out[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        U[k] = p[k];
+      const T *F = Fb + cl * 12 * NF;
+      direction_pass<N, T, UNI, VISC, 0>(A, tb, U, Nb[(cl * 6 + 0) * NF + r], Nb[(cl * 6 + 1) * NF + r],
+                                         VISC ? Nd[(cl * 6 + 0) * NF + r] : T(0),
+                                         VISC ? Nd[(cl * 6 + 1) * NF + r] : T(0), s_nbr[cl * 6 + 0] < 0,
+                                         s_nbr[cl * 6 + 1] < 0, r, F, F + 2 * NF, Gb + cl * 4 * NQ + N * r, 1,
+                                         out);
+      T *z = Qb + cl * NQ + N * r;
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        z[k] = out[k];
+    }
+  __syncthreads();
+
+  // ---- phase 3: y-direction terms
+  for (int w = tid; w < ncell * NF; w += NT)
+    {
+      const int cl = w / NF, r = w % NF;
+      const int off = (r % N) + NF * (r / N);
+      const T  *p   = Ub + cl * NQ + off;
+      T         U[N], out[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        U[k] = p[k * N];
+      const T *F = Fb + cl * 12 * NF + 4 * NF;
+      direction_pass<N, T, UNI, VISC, 1>(A, tb, U, Nb[(cl * 6 + 2) * NF + r], Nb[(cl * 6 + 3) * NF + r],
+                                         VISC ? Nd[(cl * 6 + 2) * NF + r] : T(0),
+                                         VISC ? Nd[(cl * 6 + 3) * NF + r] : T(0), s_nbr[cl * 6 + 2] < 0,
+                                         s_nbr[cl * 6 + 3] < 0, r, F, F + 2 * NF, Gb + (cl * 4 + 1) * NQ + off, N,
+                                         out);
+      T *z = Qb + cl * NQ + off;
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        z[k * N] += out[k];
+    }
+  __syncthreads();
+
+  // ---- phase 4: z-direction terms, 1/det J, and the Runge-Kutta update of
+  //      the pencil straight from registers
+  for (int w = tid; w < ncell * NF; w += NT)
+    {
+      const int cl = w / NF, r = w % NF;
+      const T  *p  = Ub + cl * NQ + r;
+      T         U[N], out[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        U[k] = p[k * NF];
+      const T *F = Fb + cl * 12 * NF + 8 * NF;
+      const T *G = Gb + cl * 4 * NQ;
+      direction_pass<N, T, UNI, VISC, 2>(A, tb, U, Nb[(cl * 6 + 4) * NF + r], Nb[(cl * 6 + 5) * NF + r],
+                                         VISC ? Nd[(cl * 6 + 4) * NF + r] : T(0),
+                                         VISC ? Nd[(cl * 6 + 5) * NF + r] : T(0), s_nbr[cl * 6 + 4] < 0,
+                                         s_nbr[cl * 6 + 5] < 0, r, F, F + 2 * NF, G + 2 * NQ + r, NF, out);
+      const T        *z  = Qb + cl * NQ + r;
+      const long long gb = (cell0 + cl) * NQ + r;
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        {
+          T zz = z[k * NF] + out[k];
+          if (!UNI)
+            zz *= G[3 * NQ + r + k * NF];
+          const double    kd = to_double<T>(zz);
+          const long long gi = gb + k * NF;
+          if (A.mode == kModeStage)
+            {
+              const double u = __ldcs(A.u_in + gi);
+              A.u_out[gi]    = fma(A.b, kd, u);
+              A.r_out[gi]    = fma(A.a, kd, u);
+            }
+          else if (A.mode == kModeLastStage)
+            A.u_out[gi] = fma(A.b, kd, __ldcs(A.u_in + gi));
+          else
+            A.r_out[gi] = A.out_scale * kd;
+        }
+    }
+}
+
+template <int N, typename T, bool UNI, bool VISC>
+__global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS) stage_gauss_kernel(const StageArgs A)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  stage_gauss_cta<N, T, UNI, VISC>(A, A.cell_begin + (long long)blockIdx.x * StageShape<N, T, UNI, VISC>::C,
+                                   smem_raw);
+}
+
+template <int N, typename T, bool UNI, bool VISC>
+cudaError_t launch_stage_gauss_t(const StageArgs &args, cudaStream_t stream)
+{
+  using SH = StageShape<N, T, UNI, VISC>;
+  static unsigned long long configured = 0;
+  int                       dev        = 0;
+  cudaError_t               e          = cudaGetDevice(&dev);
+  if (e != cudaSuccess)
+    return e;
+  if (dev >= 64 || !((configured >> dev) & 1ull))
+    {
+      e = cudaFuncSetAttribute(stage_gauss_kernel<N, T, UNI, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               SH::SMEM);
+      if (e != cudaSuccess)
+        return e;
+      if (dev < 64)
+        configured |= 1ull << dev;
+    }
+  const long long blocks = (args.n_cells - args.cell_begin + SH::C - 1) / SH::C;
+  stage_gauss_kernel<N, T, UNI, VISC><<<(unsigned)blocks, SH::THREADS, SH::SMEM, stream>>>(args);
+  return cudaGetLastError();
+}
+
+template <int N, typename T>
+cudaError_t launch_stage_gauss_n(const StageArgs &args, cudaStream_t stream)
+{
+  if (args.visc)
+    return launch_stage_gauss_t<N, T, false, true>(args, stream);
+  return args.uniform ? launch_stage_gauss_t<N, T, true, false>(args, stream)
+                      : launch_stage_gauss_t<N, T, false, false>(args, stream);
+}
+
+template <typename T>
+cudaError_t launch_stage_gauss_any(int n, const StageArgs &args, cudaStream_t stream)
+{
+  switch (n)
+    {
+      case 2: return launch_stage_gauss_n<2, T>(args, stream);
+      case 3: return launch_stage_gauss_n<3, T>(args, stream);
+      case 4: return launch_stage_gauss_n<4, T>(args, stream);
+      case 5: return launch_stage_gauss_n<5, T>(args, stream);
+      case 6: return launch_stage_gauss_n<6, T>(args, stream);
+      case 7: return launch_stage_gauss_n<7, T>(args, stream);
+      default: return cudaErrorInvalidValue;
+    }
+}
+} // namespace adv

@@ -1,0 +1,95 @@
+// Instantiations of the collocation-form stage kernel with a binary64
+// operator, and the change of basis of the fused LSRK loop.
+#include "stage_gauss.cuh"
+
+namespace adv
+{
+namespace
+{
+// u <- (M x M x M) u per cell, M = S (to the Gauss points) or S^-1, through
+// shared memory: one thread per pencil, C cells per CTA
+template <int N, bool TO_GAUSS>
+__global__ void __launch_bounds__(StageShape<N, double, true, false>::THREADS)
+  basis_kernel(double *u, long long cell_begin, long long cell_end)
+{
+  using SH         = StageShape<N, double, true, false>;
+  constexpr int C  = SH::C;
+  constexpr int NQ = SH::NQ;
+  constexpr int NF = SH::NF;
+  constexpr int NT = SH::THREADS;
+  __shared__ double    buf[C * NQ];
+  const DevTables<double> &tb    = tab<double>(N);
+  const long long          cell0 = cell_begin + (long long)blockIdx.x * C;
+  const int                ncell = (int)min((long long)C, cell_end - cell0);
+  const int                tid   = threadIdx.x;
+  double                  *g     = u + cell0 * NQ;
+  for (int i = tid; i < ncell * NQ; i += NT)
+    buf[i] = g[i];
+  __syncthreads();
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    {
+      for (int w = tid; w < ncell * NF; w += NT)
+        {
+          const int cl = w / NF, r = w % NF;
+          const int off = d == 0 ? N * r : d == 1 ? (r % N) + NF * (r / N) : r;
+          const int st  = d == 0 ? 1 : d == 1 ? N : NF;
+          double   *p   = buf + cl * NQ + off;
+          double    in[N], out[N];
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            in[k] = p[k * st];
+          if (TO_GAUSS)
+            sweep2<N, double, false>(tb.S, tb.S_eo, in, out);
+          else
+            sweep2<N, double, false>(tb.Si, tb.Si_eo, in, out);
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            p[k * st] = out[k];
+        }
+      __syncthreads();
+    }
+  for (int i = tid; i < ncell * NQ; i += NT)
+    g[i] = buf[i];
+}
+
+template <int N>
+cudaError_t launch_basis_n(double *u, long long cell_begin, long long cell_end, bool to_gauss, cudaStream_t s)
+{
+  using SH               = StageShape<N, double, true, false>;
+  const long long blocks = (cell_end - cell_begin + SH::C - 1) / SH::C;
+  if (blocks <= 0)
+    return cudaSuccess;
+  if (to_gauss)
+    basis_kernel<N, true><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end);
+  else
+    basis_kernel<N, false><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end);
+  return cudaGetLastError();
+}
+} // namespace
+
+cudaError_t upload_tables_gauss64(const DevTables<double> *d, const DevTables<float> *f)
+{
+  return upload_tables_local(d, f);
+}
+
+cudaError_t launch_stage_gauss_fp64(int n, const StageArgs &args, cudaStream_t stream)
+{
+  return launch_stage_gauss_any<double>(n, args, stream);
+}
+
+cudaError_t launch_basis_change(int n, double *u, long long cell_begin, long long cell_end, bool to_gauss,
+                                cudaStream_t stream)
+{
+  switch (n)
+    {
+      case 2: return launch_basis_n<2>(u, cell_begin, cell_end, to_gauss, stream);
+      case 3: return launch_basis_n<3>(u, cell_begin, cell_end, to_gauss, stream);
+      case 4: return launch_basis_n<4>(u, cell_begin, cell_end, to_gauss, stream);
+      case 5: return launch_basis_n<5>(u, cell_begin, cell_end, to_gauss, stream);
+      case 6: return launch_basis_n<6>(u, cell_begin, cell_end, to_gauss, stream);
+      case 7: return launch_basis_n<7>(u, cell_begin, cell_end, to_gauss, stream);
+      default: return cudaErrorInvalidValue;
+    }
+}
+} // namespace adv

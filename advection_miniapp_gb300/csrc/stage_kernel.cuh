@@ -280,32 +280,13 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
     }
 }
 
-// One CTA's work: cells cell0 .. cell0 + C - 1 of the mesh described by A,
-// with the dynamic shared memory of the launch.  Shared by the single-mesh
-// kernel and the batched multi-mesh kernel of the serving loop.
-template <int N, typename T, bool UNI, bool VISC>
-__device__ __forceinline__ void stage_cta(const StageArgs &A, const long long cell0, unsigned char *smem_raw)
+// Neighbour cells (-1 on boundary faces) and face ids of the cells
+// cell0 .. cell0 + ncell - 1: s_nbr / s_face [cell][6] with faces ordered
+// (x low, x high, y low, y high, z low, z high).
+__device__ __forceinline__ void cell_neighbours(const StageArgs &A, long long cell0, int ncell, int *s_nbr,
+                                                int *s_face, int tid, int nthreads)
 {
-  using SH         = StageShape<N, T, UNI, VISC>;
-  constexpr int C  = SH::C;
-  constexpr int NQ = SH::NQ;
-  constexpr int NF = SH::NF;
-  constexpr int NT = SH::THREADS;
-  T   *Ub     = reinterpret_cast<T *>(smem_raw); // [C][NQ] nodal -> Gauss values
-  T   *Qb     = Ub + C * NQ;                     // [C][NQ] accumulated Z, then k
-  T   *Nb     = Qb + C * NQ;                     // [C][6][NF] neighbour face values
-  T   *Gb     = Nb + C * 6 * NF;                 // field: [C][4][NQ] cell geometry
-  T   *Fb     = Gb + (UNI ? 0 : C * 4 * NQ);     // field: [C][6][2][NF] face coefficients
-  T   *Nd     = Fb + (UNI ? 0 : C * 12 * NF);    // viscous: [C][6][NF] neighbour normal derivatives
-  int *s_nbr  = reinterpret_cast<int *>(Nd + (VISC ? C * 6 * NF : 0)); // [C][6] neighbour or -1
-  int *s_face = s_nbr + C * 6;                                          // [C][6] face id
-
-  const DevTables<T> &tb    = tab<T>(N);
-  const int           tid   = threadIdx.x;
-  const int           ncell = (int)min((long long)C, A.n_cells - cell0);
-
-  // ---- phase 0a: neighbour cells and face ids of the CTA's cells
-  for (int i = tid; i < ncell * 6; i += NT)
+  for (int i = tid; i < ncell * 6; i += nthreads)
     {
       const int       cl = i / 6, j = i % 6, d = j >> 1, s = j & 1;
       const long long c  = cell0 + cl;
@@ -334,29 +315,65 @@ __device__ __forceinline__ void stage_cta(const StageArgs &A, const long long ce
           s_nbr[i] = (int)(jx + (long long)nx * (jy + (long long)ny * jz));
         }
     }
+}
+
+// Field case: asynchronous copies of the cell geometry (16-byte chunks) and
+// the face coefficients (8-byte chunks) into shared memory, committed as one
+// group; the caller waits with __pipeline_wait_prior(0) before using them.
+template <int N, typename T>
+__device__ __forceinline__ void geometry_async(const StageArgs &A, long long cell0, int ncell, const int *s_face,
+                                               T *Gb, T *Fb, int tid, int nthreads)
+{
+  constexpr int NQ  = N * N * N;
+  constexpr int NF  = N * N;
+  const char   *geo = reinterpret_cast<const char *>(static_cast<const T *>(A.cell_geo) + cell0 * 4 * NQ);
+  const int     n16 = ncell * 4 * NQ * (int)sizeof(T) / 16;
+  for (int i = tid; i < n16; i += nthreads)
+    __pipeline_memcpy_async(reinterpret_cast<char *>(Gb) + 16 * i, geo + 16 * i, 16);
+  constexpr int F8 = 2 * NF * (int)sizeof(T) / 8; // 8-byte chunks per cell-face
+  for (int i = tid; i < ncell * 6 * F8; i += nthreads)
+    {
+      const int cf = i / F8, e = i % F8;
+      const int d  = (cf % 6) >> 1;
+      const T  *F  = static_cast<const T *>(d == 0 ? A.face_geo[0] : d == 1 ? A.face_geo[1] : A.face_geo[2]);
+      __pipeline_memcpy_async(reinterpret_cast<char *>(Fb + cf * 2 * NF) + 8 * e,
+                              reinterpret_cast<const char *>(F + (size_t)s_face[cf] * 2 * NF) + 8 * e, 8);
+    }
+  __pipeline_commit();
+}
+
+// One CTA's work: cells cell0 .. cell0 + C - 1 of the mesh described by A,
+// with the dynamic shared memory of the launch.  Shared by the single-mesh
+// kernel and the batched multi-mesh kernel of the serving loop.
+template <int N, typename T, bool UNI, bool VISC>
+__device__ __forceinline__ void stage_cta(const StageArgs &A, const long long cell0, unsigned char *smem_raw)
+{
+  using SH         = StageShape<N, T, UNI, VISC>;
+  constexpr int C  = SH::C;
+  constexpr int NQ = SH::NQ;
+  constexpr int NF = SH::NF;
+  constexpr int NT = SH::THREADS;
+  T   *Ub     = reinterpret_cast<T *>(smem_raw); // [C][NQ] nodal -> Gauss values
+  T   *Qb     = Ub + C * NQ;                     // [C][NQ] accumulated Z, then k
+  T   *Nb     = Qb + C * NQ;                     // [C][6][NF] neighbour face values
+  T   *Gb     = Nb + C * 6 * NF;                 // field: [C][4][NQ] cell geometry
+  T   *Fb     = Gb + (UNI ? 0 : C * 4 * NQ);     // field: [C][6][2][NF] face coefficients
+  T   *Nd     = Fb + (UNI ? 0 : C * 12 * NF);    // viscous: [C][6][NF] neighbour normal derivatives
+  int *s_nbr  = reinterpret_cast<int *>(Nd + (VISC ? C * 6 * NF : 0)); // [C][6] neighbour or -1
+  int *s_face = s_nbr + C * 6;                                          // [C][6] face id
+
+  const DevTables<T> &tb    = tab<T>(N);
+  const int           tid   = threadIdx.x;
+  const int           ncell = (int)min((long long)C, A.n_cells - cell0);
+
+  // ---- phase 0a: neighbour cells and face ids of the CTA's cells
+  cell_neighbours(A, cell0, ncell, s_nbr, s_face, tid, NT);
   __syncthreads();
 
   // ---- phase 0b: curved meshes / variable velocity: start the asynchronous
-  //      copies of the cell geometry (16-byte chunks) and the face
-  //      coefficients (8-byte chunks) into shared memory; they land while the
-  //      interpolation sweeps below run
+  //      copies of the geometry; they land while the sweeps below run
   if (!UNI)
-    {
-      const char *geo = reinterpret_cast<const char *>(static_cast<const T *>(A.cell_geo) + cell0 * 4 * NQ);
-      const int   n16 = ncell * 4 * NQ * (int)sizeof(T) / 16;
-      for (int i = tid; i < n16; i += NT)
-        __pipeline_memcpy_async(reinterpret_cast<char *>(Gb) + 16 * i, geo + 16 * i, 16);
-      constexpr int F8 = 2 * NF * (int)sizeof(T) / 8; // 8-byte chunks per cell-face
-      for (int i = tid; i < ncell * 6 * F8; i += NT)
-        {
-          const int cf = i / F8, e = i % F8;
-          const int d  = (cf % 6) >> 1;
-          const T  *F  = static_cast<const T *>(d == 0 ? A.face_geo[0] : d == 1 ? A.face_geo[1] : A.face_geo[2]);
-          __pipeline_memcpy_async(reinterpret_cast<char *>(Fb + cf * 2 * NF) + 8 * e,
-                                  reinterpret_cast<const char *>(F + (size_t)s_face[cf] * 2 * NF) + 8 * e, 8);
-        }
-      __pipeline_commit();
-    }
+    geometry_async<N, T>(A, cell0, ncell, s_face, Gb, Fb, tid, NT);
 
   // ---- phase 1: own values loaded as z-pencils and interpolated along z;
   //      neighbour face layers loaded as rows along their first tangential

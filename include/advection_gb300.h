@@ -56,6 +56,16 @@ enum { ADV_LSRK_3_3 = 0, ADV_LSRK_5_4 = 1, ADV_LSRK_7_4 = 2, ADV_LSRK_9_5 = 3 };
  * Run-time replacement of the reference's compile-time parameter block
  * (advection_solver.cc:55-123; degree was a template argument there).
  */
+/* Basis the fused step loop (adv_lsrk_steps / adv_lsrk_step) runs its
+ * stages in.  The result is the same polynomial to round-off: AUTO picks the
+ * faster form for the precision, NODAL keeps the Gauss-Lobatto nodal values of
+ * the reference, COLLOCATION changes the solution to the values at the Gauss
+ * points on entry and back on exit and skips the interpolation and
+ * inverse-mass sweeps in every stage. */
+#define ADV_FORM_AUTO 0
+#define ADV_FORM_NODAL 1
+#define ADV_FORM_COLLOCATION 2
+
 typedef struct adv_config
 {
   int32_t degree;            /* FE_DGQ degree k, 1..6 (n = k+1 points per direction) */
@@ -78,7 +88,8 @@ typedef struct adv_config
   double  ic_params[8];      /* sine-Gauss: phase p[3]; blob: centre c[3], width w */
   /* ---- fields below have no counterpart in the oracle's configuration ---- */
   int32_t precision;         /* ADV_PRECISION_*: FP64, or FP32 operator with FP64 vectors */
-  int32_t reserved1[7];
+  int32_t fused_form;        /* ADV_FORM_*: basis of the stages inside adv_lsrk_steps */
+  int32_t reserved1[6];
 } adv_config;
 
 typedef struct adv_handle adv_handle;
