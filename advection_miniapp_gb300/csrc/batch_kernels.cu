@@ -4,18 +4,23 @@
 // (same degree and operator precision; affine periodic meshes with constant
 // velocity, the serving mix).  The CTAs are mapped to (solve, first cell)
 // pairs by two device tables; each CTA builds its solve's stage arguments in
-// shared memory and runs the same per-CTA code as the single-mesh kernel, so
-// a solve computes bit-for-bit the same values alone and inside a batch.
+// shared memory and runs the same per-CTA code as the single-mesh fused step
+// loop in the form that loop picks by default (collocation for the FP64
+// operator, nodal for the FP32 one), so a solve computes bit-for-bit the same
+// values alone, inside a batch, and through adv_lsrk_steps.
 // Slot tables live in device memory so that a captured CUDA graph of a tick
 // (steps x stages launches + one step-advance launch per step) stays valid
 // while solves join and leave the batch.
 #include "batch_kernels.h"
-#include "stage_kernel.cuh"
+#include "stage_gauss.cuh"
 
 namespace adv
 {
 namespace
 {
+template <typename T>
+constexpr bool kBatchCollocation = sizeof(T) == sizeof(double);
+
 template <int N, typename T>
 __global__ void __launch_bounds__(StageShape<N, T, true, false>::THREADS) batch_stage_kernel(const BatchLaunch L)
 {
@@ -68,7 +73,10 @@ __global__ void __launch_bounds__(StageShape<N, T, true, false>::THREADS) batch_
   __syncthreads();
   if (skip)
     return;
-  stage_cta<N, T, true, false>(sA, cell0, smem_raw);
+  if constexpr (kBatchCollocation<T>)
+    stage_gauss_cta<N, T, true, false>(sA, cell0, smem_raw);
+  else
+    stage_cta<N, T, true, false>(sA, cell0, smem_raw);
 }
 
 __global__ void batch_advance_kernel(BatchSlot *slots, const int *n_slots)
@@ -97,6 +105,11 @@ cudaError_t launch_batch_t(const BatchLaunch &L, int cta_capacity, cudaStream_t 
 cudaError_t upload_tables_batch(const DevTables<double> *d, const DevTables<float> *f)
 {
   return upload_tables_local(d, f);
+}
+
+bool batch_collocation(int precision)
+{
+  return precision == 0;
 }
 
 int batch_cells_per_cta(int n)

@@ -33,6 +33,8 @@ struct BatchLaunch
 
 cudaError_t upload_tables_batch(const DevTables<double> *d, const DevTables<float> *f);
 int         batch_cells_per_cta(int n);
+// whether the group's vectors hold Gauss-point values (collocation form)
+bool        batch_collocation(int precision);
 // sets the kernel's shared-memory limit on the current device (call before capturing a graph)
 cudaError_t prepare_batch_stage(int n, int precision);
 cudaError_t launch_batch_stage(int n, int precision, const BatchLaunch &L, int cta_capacity, cudaStream_t s);

@@ -230,6 +230,12 @@ int retire(adv_server *S, SGroup &g, int64_t id)
 {
   SReq &q = S->reqs[id];
   int   nb = 0;
+  if (adv::batch_collocation(g.precision))
+    {
+      const long long cells = (long long)q.n * q.n * q.n;
+      ADV_CUDA(adv::launch_basis_change(q.npts, q.u, 0, cells, false, g.stream));
+      ++S->launches;
+    }
   ADV_CUDA(adv::launch_l2_error(q.diag, q.u, q.t_end, g.d_partials, &nb, g.stream));
   ++S->launches;
   std::vector<double> part(3 * nb);
@@ -269,6 +275,12 @@ int admit(adv_server *S, int64_t id)
   ADV_CUDA(cudaMallocAsync((void **)&q.k, nb, g->stream));
   ADV_CUDA(adv::launch_project(q.diag, 0.0, q.u, g->stream));
   ++S->launches;
+  if (adv::batch_collocation(q.precision))
+    {
+      const long long cells = (long long)q.n * q.n * q.n;
+      ADV_CUDA(adv::launch_basis_change(q.npts, q.u, 0, cells, true, g->stream));
+      ++S->launches;
+    }
   q.state   = 1;
   q.t_admit = now_s();
   g->members.push_back(id);
