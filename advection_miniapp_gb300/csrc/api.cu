@@ -347,15 +347,18 @@ int launch(adv_handle *h, const adv::StageArgs &A, cudaStream_t s)
 }
 
 // Basis of the fused step loop: the collocation form wherever it is the
-// faster one (measured: the FP64 operator, whose stages are bound by the
-// FP64 pipe and lose about 40 % of their instructions)
+// faster one.  Measured on GB300: the FP64 operator (bound by the FP64 pipe,
+// about 40 % fewer instructions; 1.68x at degree 4 on 64^3 curved cells) and
+// the FP32 operator with diffusion (1.45x at degree 5); the FP32 advection
+// operator is bound by memory latency and keeps the nodal form, whose
+// neighbour reads are face layers rather than whole cells.
 bool use_collocation(const adv_handle &h)
 {
   if (h.cfg.fused_form == ADV_FORM_NODAL)
     return false;
   if (h.cfg.fused_form == ADV_FORM_COLLOCATION)
     return true;
-  return h.cfg.precision == ADV_PRECISION_FP64;
+  return h.cfg.precision == ADV_PRECISION_FP64 || h.cfg.diffusion != 0.0;
 }
 
 int ensure_scratch(adv_handle *h, int i)

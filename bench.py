@@ -75,18 +75,25 @@ def _sweep_cost(n, anti):
     return inst, flops
 
 
-def fp_work_per_cell(n, curved=True, stage=True):
+def fp_work_per_cell(n, curved=True, stage=True, collocation=False):
     """(FP instructions, flops with FMA = 2) of one fused stage per cell,
-    phase by phase as in stage_kernel: interpolation sweeps of the own cell
-    (3 x n^2 pencils) and of the six neighbour layers (2 x 6n rows), three
-    direction passes per pencil (two face traces, flux, volume term with the
-    weighted derivative, two lifts), 1/det J, three inverse-mass sweeps and the
-    two-FMA update per DoF."""
+    phase by phase as in the kernels.  Nodal form (stage_kernel.cuh):
+    interpolation sweeps of the own cell (3 x n^2 pencils) and of the six
+    neighbour layers (2 x 6n rows), three direction passes per pencil (two
+    face traces, flux, volume term with the weighted derivative, two lifts),
+    1/det J, three inverse-mass sweeps and the two-FMA update per DoF.
+    Collocation form (stage_gauss.cuh): no interpolation or inverse-mass
+    sweeps; the neighbours' face values are n-term contractions at the 6 n^2
+    face points."""
     si, sf = _sweep_cost(n, anti=False)
     di, df = _sweep_cost(n, anti=True)
     p = n * n
-    inst = 3 * p * si + 12 * n * si
-    flops = 3 * p * sf + 12 * n * sf
+    if collocation:
+        inst = 6 * p * n
+        flops = 6 * p * (2 * n - 1)
+    else:
+        inst = 3 * p * si + 12 * n * si
+        flops = 3 * p * sf + 12 * n * sf
     pass_i = 2 * n + 4 + (n if curved else n) + di + 2 * n
     pass_f = 2 * (2 * n - 1) + 6 + n + df + 4 * n
     inst += 3 * p * pass_i
@@ -94,12 +101,25 @@ def fp_work_per_cell(n, curved=True, stage=True):
     if curved:
         inst += n ** 3
         flops += n ** 3
-    inst += 3 * p * si
-    flops += 3 * p * sf
+    if not collocation:
+        inst += 3 * p * si
+        flops += 3 * p * sf
     upd = 2 if stage else 1
     inst += upd * n ** 3
     flops += 2 * upd * n ** 3
     return inst, flops
+
+
+# DRAM bytes (read + write) per DoF of one stage launch of the dominant
+# kernels, from ncu captures of the 40^3 curved degree-4 case (8,000,000 DoFs,
+# vectors and geometry larger than L2; profiles/ has the commands), scaled to
+# the workload by the DoF count
+NCU_TRAFFIC_PER_DOF = {"fp64": None, "fp32": (296.933120e6 + 94.805248e6) / 8.0e6}
+
+
+def traffic(per_dof, n_dofs):
+    """DRAM bytes of one stage launch of the workload from the ncu figure per DoF."""
+    return None if per_dof is None else round(per_dof * n_dofs)
 
 
 def bytes_per_dof_step():
@@ -224,15 +244,19 @@ def reference_arm(args):
 # our arm
 # --------------------------------------------------------------------------
 def time_steps(torch, op, adv, u, r, k, dt, steps, warmup, stream):
+    """Seconds of `steps` fused steps after `warmup` untimed ones, and the
+    kernel launches inside the timed region."""
     with torch.cuda.stream(stream):
         op.lsrk_steps(adv.LSRK_5_4, 0.0, dt, warmup, u, r, k, stream=stream)
         stream.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = op.launch_count()
         e0.record(stream)
         op.lsrk_steps(adv.LSRK_5_4, warmup * dt, dt, steps, u, r, k, stream=stream)
         e1.record(stream)
         e1.synchronize()
-    return e0.elapsed_time(e1) / 1e3
+        n1 = op.launch_count()
+    return e0.elapsed_time(e1) / 1e3, n1 - n0
 
 
 def run_precision(torch, adv, precision, args, stream, sampler_index):
@@ -242,10 +266,8 @@ def run_precision(torch, adv, precision, args, stream, sampler_index):
     op.project_initial(u)
     r, k = op.initialize_dof_vector(), op.initialize_dof_vector()
     torch.cuda.synchronize()
-    launches0 = op.launch_count()
     with ClockSampler(sampler_index) as clk:
-        sec = time_steps(torch, op, adv, u, r, k, dt, args.steps, args.warmup, stream)
-    launches = op.launch_count() - launches0 - STAGES * args.warmup
+        sec, launches = time_steps(torch, op, adv, u, r, k, dt, args.steps, args.warmup, stream)
     err, nrm = op.l2_error(u, (args.warmup + args.steps) * dt)
     return dict(op=op, u=u, r=r, k=k, dt=dt, seconds=sec, launches=launches, rel_l2=err / nrm,
                 clocks=clk.summary())
@@ -344,11 +366,17 @@ def ours(args):
         return
 
     n = 5
+    # stage launch durations: the timed region over its stage launches (the
+    # FP64 run adds two basis changes per lsrk_steps call, under 1 % of it)
     launch64 = r64["seconds"] / (STAGES * args.steps)
     launch32 = r32["seconds"] / (STAGES * args.steps)
-    # average over the 5 launches of a step: 4 stages with 2 update FMAs per DoF, the last with 1
-    inst = (4 * fp_work_per_cell(n)[0] + fp_work_per_cell(n, stage=False)[0]) / STAGES
-    flops = (4 * fp_work_per_cell(n)[1] + fp_work_per_cell(n, stage=False)[1]) / STAGES
+    # average over the 5 launches of a step: 4 stages with 2 update FMAs per DoF, the last with 1;
+    # FP64 runs the collocation form, FP32 the nodal form (the library's default choice)
+    inst = (4 * fp_work_per_cell(n, collocation=True)[0]
+            + fp_work_per_cell(n, stage=False, collocation=True)[0]) / STAGES
+    flops = (4 * fp_work_per_cell(n, collocation=True)[1]
+             + fp_work_per_cell(n, stage=False, collocation=True)[1]) / STAGES
+    flops32 = (4 * fp_work_per_cell(n)[1] + fp_work_per_cell(n, stage=False)[1]) / STAGES
     vec_bytes_launch = bytes_per_dof_step() / STAGES * n_dofs
     # FP64 instructions of any kind (FMA, add, mul) take one issue slot of the
     # FP64 pipe; expressed as FMA-equivalent TFLOP/s (2 flops per slot) they
@@ -388,7 +416,9 @@ def ours(args):
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "rel_l2_error": r64["rel_l2"],
         "roofline": {"bound": "fp64", "achieved": round(achieved64, 4), "peak": round(fp64_peak, 4),
-                     "unit": "TFLOP/s", "frac": round(achieved64 / fp64_peak, 4), "traffic": None,
+                     "unit": "TFLOP/s", "frac": round(achieved64 / fp64_peak, 4),
+                     "traffic": traffic(NCU_TRAFFIC_PER_DOF["fp64"], n_dofs),
+                     "form": "collocation (Gauss-point values inside lsrk_steps)",
                      "peak_source": "FP64 FMA microbenchmark (adv_measure_fma_peak) on this GPU",
                      "achieved_definition": "2 x FP64 instructions per second (each FP64 add/mul/FMA takes one "
                                             "FMA issue slot); algorithmic_tflops counts FMA = 2, add/mul = 1",
@@ -404,10 +434,11 @@ def ours(args):
             "l2_error_ratio": round(r32["rel_l2"] / r64["rel_l2"], 6),
             "ms_per_step": round(sec32 / args.steps * 1e3, 4),
             "roofline": {"bound": "hbm", "achieved": round(achieved32_hbm, 2), "peak": hbm_peak, "unit": "GB/s",
-                         "frac": round(achieved32_hbm / hbm_peak, 4), "traffic": None,
+                         "frac": round(achieved32_hbm / hbm_peak, 4),
+                         "traffic": traffic(NCU_TRAFFIC_PER_DOF["fp32"], n_dofs), "form": "nodal",
                          "geometry_gbs": round(geo32, 2),
                          "frac_with_geometry": round((achieved32_hbm + geo32) / hbm_peak, 4),
-                         "fp32_flops_tflops": round(flops * n_cells / launch32 / 1e12, 3),
+                         "fp32_flops_tflops": round(flops32 * n_cells / launch32 / 1e12, 3),
                          "fp32_peak_tflops": round(fp32_peak, 3), "launch_ms": round(launch32 * 1e3, 4)},
             "clocks": r32["clocks"]},
         "e2e": e2e,
