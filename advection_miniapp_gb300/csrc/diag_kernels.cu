@@ -52,37 +52,52 @@ __device__ void tsweep(const double *A, int mo, int ni, int d, int d0, int d1, i
   __syncthreads();
 }
 
-// support points of the curved mapping, component c, into X (n^3)
-__device__ void support_component(const DiagArgs &g, const double lo[3], int c, double *X)
+// support points of a curved cell, the three components X[c * n^3 + i]; each
+// sine of the deformation depends on one coordinate, so the 3n values
+// sin(2 pi s_d) at the nodes along each direction (sn) serve all n^3 points
+// (the same arithmetic as deform_dev)
+__device__ void support_points(const DiagArgs &g, const double lo[3], double *X, double *sn)
 {
-  const int n = g.n, nq = n * n * n;
+  const double kPi = 3.14159265358979323846;
+  const int    n = g.n, nq = n * n * n;
+  for (int i = threadIdx.x; i < 3 * n; i += blockDim.x)
+    {
+      const int    d = i / n, a = i % n;
+      const double x = lo[d] + g.h[d] * g.gl[a];
+      sn[i]          = sin(2.0 * kPi * ((x - g.lo[d]) / g.L[d]));
+    }
+  __syncthreads();
   for (int i = threadIdx.x; i < nq; i += blockDim.x)
     {
-      const int    a = i % n, b = (i / n) % n, cc = i / (n * n);
-      const double p[3] = {lo[0] + g.h[0] * g.gl[a], lo[1] + g.h[1] * g.gl[b], lo[2] + g.h[2] * g.gl[cc]};
-      double       y[3];
-      deform_dev(g.deformation, g.lo, g.L, p, y);
-      X[i] = y[c];
+      const int a[3] = {i % n, (i / n) % n, i / (n * n)};
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        {
+          const int    c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+          const double p  = lo[c] + g.h[c] * g.gl[a[c]];
+          X[c * nq + i]   = p + g.deformation * g.L[c] * sn[c1 * n + a[c1]] * sn[c2 * n + a[c2]];
+        }
     }
   __syncthreads();
 }
 
 struct Scratch
 {
-  double *X, *A, *Az, *B, *By, *Bz;
+  double *X, *A, *Az, *B, *By, *Bz, *sn;
 };
 
 // position x[c][p] and Jacobian J[3c + j][p] at the m^3 points of the 1D rule
-// with nodal-basis values V and derivatives W (m x n); curved cells only
-__device__ void map_points(const DiagArgs &g, const double lo[3], int m, const double *V, const double *W,
-                           double *x, double *J, const Scratch &s)
+// with nodal-basis values V and derivatives W (m x n), from the support
+// points in s.X; curved cells only
+__device__ void map_points(const DiagArgs &g, int m, const double *V, const double *W, double *x, double *J,
+                           const Scratch &s)
 {
-  const int n = g.n, m3 = m * m * m;
+  const int n = g.n, m3 = m * m * m, nq = n * n * n;
   for (int c = 0; c < 3; ++c)
     {
-      support_component(g, lo, c, s.X);
-      tsweep(V, m, n, 2, n, n, n, s.X, s.A);
-      tsweep(W, m, n, 2, n, n, n, s.X, s.Az);
+      const double *X = s.X + c * nq;
+      tsweep(V, m, n, 2, n, n, n, X, s.A);
+      tsweep(W, m, n, 2, n, n, n, X, s.Az);
       tsweep(V, m, n, 1, n, n, m, s.A, s.B);
       tsweep(W, m, n, 1, n, n, m, s.A, s.By);
       tsweep(V, m, n, 1, n, n, m, s.Az, s.Bz);
@@ -161,9 +176,9 @@ __device__ void block_reduce3(double v0, double v1, double v2, double *out)
     }
 }
 
-// shared-memory layout (doubles): X, A, Az, B, By, Bz, x[3], J[9], U, T1, T2, T3
-constexpr int kSmemDoubles = kMaxN3 + 2 * kMaxP * kMaxP * 7 + 3 * kMaxP * kMaxP * 7 + 12 * kMaxP3 + kMaxN3 +
-                             3 * kMaxP3;
+// shared-memory layout (doubles): X[3], A, Az, B, By, Bz, x[3], J[9], U, T1, T2, T3, sn
+constexpr int kSmemDoubles = 3 * kMaxN3 + 2 * kMaxP * kMaxP * 7 + 3 * kMaxP * kMaxP * 7 + 12 * kMaxP3 + kMaxN3 +
+                             3 * kMaxP3 + 3 * kMaxP;
 
 struct Layout
 {
@@ -172,7 +187,7 @@ struct Layout
   __device__ explicit Layout(double *base)
   {
     s.X  = base;
-    s.A  = s.X + kMaxN3;
+    s.A  = s.X + 3 * kMaxN3;
     s.Az = s.A + kMaxP * kMaxP * 7;
     s.B  = s.Az + kMaxP * kMaxP * 7;
     s.By = s.B + kMaxP * kMaxP * 7;
@@ -183,6 +198,7 @@ struct Layout
     T1   = U + kMaxN3;
     T2   = T1 + kMaxP3;
     T3   = T2 + kMaxP3;
+    s.sn = T3 + kMaxP3;
   }
 };
 
@@ -196,7 +212,10 @@ __global__ void __launch_bounds__(kDiagThreads) project_kernel(const DiagArgs g,
       double lo[3];
       cell_origin(g, c, lo);
       if (g.curved)
-        map_points(g, lo, n, g.S, g.Sd, L.x, L.J, L.s);
+        {
+          support_points(g, lo, L.s.X, L.s.sn);
+          map_points(g, n, g.S, g.Sd, L.x, L.J, L.s);
+        }
       for (int q = threadIdx.x; q < nq; q += blockDim.x)
         {
           double xp[3];
@@ -227,7 +246,10 @@ __global__ void __launch_bounds__(kDiagThreads)
       double lo[3];
       cell_origin(g, c, lo);
       if (g.curved)
-        map_points(g, lo, n, g.S, g.Sd, L.x, L.J, L.s);
+        {
+          support_points(g, lo, L.s.X, L.s.sn);
+          map_points(g, n, g.S, g.Sd, L.x, L.J, L.s);
+        }
       for (int i = threadIdx.x; i < nq; i += blockDim.x)
         L.U[i] = u[c * nq + i];
       __syncthreads();
@@ -278,7 +300,10 @@ __global__ void __launch_bounds__(kDiagThreads)
       tsweep(g.SE, m, n, 1, m, n, n, L.T1, L.T2);
       tsweep(g.SE, m, n, 2, m, m, n, L.T2, L.T3);
       if (g.curved)
-        map_points(g, lo, m, g.SE, g.SEd, L.x, L.J, L.s);
+        {
+          support_points(g, lo, L.s.X, L.s.sn);
+          map_points(g, m, g.SE, g.SEd, L.x, L.J, L.s);
+        }
       for (int p = threadIdx.x; p < m3; p += blockDim.x)
         {
           double xp[3], Jp[9], Ji[9];
@@ -290,9 +315,9 @@ __global__ void __launch_bounds__(kDiagThreads)
           err += d * d * det * g.ew[p0] * g.ew[p1] * g.ew[p2];
         }
       __syncthreads();
-      // norm of the exact solution with QGauss(k+1)
+      // norm of the exact solution with QGauss(k+1) (same support points)
       if (g.curved)
-        map_points(g, lo, n, g.S, g.Sd, L.x, L.J, L.s);
+        map_points(g, n, g.S, g.Sd, L.x, L.J, L.s);
       for (int q = threadIdx.x; q < nq; q += blockDim.x)
         {
           double xp[3], Jp[9], Ji[9];
