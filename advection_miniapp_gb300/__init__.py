@@ -11,7 +11,8 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._lib import (AdvConfig, AdvError, BOUNDARY_EXACT, BOUNDARY_ZERO, FORM_AUTO, FORM_COLLOCATION, FORM_NODAL,
+from ._lib import (AdvConfig, AdvError, BOUNDARY_EXACT, BOUNDARY_ZERO, FORM_AUTO, FORM_COLLOCATION, FORM_COLLOCATION_NO_TRACES,
+                   FORM_NODAL,
                    IC_BLOB, IC_SINE_GAUSS,
                    IC_WAVE, LSRK_3_3, LSRK_5_4, LSRK_7_4, LSRK_9_5, MESH_CARTESIAN, MESH_DEFORMED,
                    PRECISION_FP32_OPERATOR, PRECISION_FP64, VELOCITY_CONSTANT, VELOCITY_ROTATING)

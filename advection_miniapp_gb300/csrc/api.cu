@@ -160,7 +160,7 @@ int validate(const adv_config &c)
 {
   if (c.degree < 1 || c.degree > 6)
     return fail(ADV_ERR_INVALID, "degree must be in 1..6");
-  if (c.fused_form < ADV_FORM_AUTO || c.fused_form > ADV_FORM_COLLOCATION)
+  if (c.fused_form < ADV_FORM_AUTO || c.fused_form > ADV_FORM_COLLOCATION_NO_TRACES)
     return fail(ADV_ERR_INVALID, "unknown fused_form");
   for (int d = 0; d < 3; ++d)
     {
@@ -356,9 +356,29 @@ bool use_collocation(const adv_handle &h)
 {
   if (h.cfg.fused_form == ADV_FORM_NODAL)
     return false;
-  if (h.cfg.fused_form == ADV_FORM_COLLOCATION)
+  if (h.cfg.fused_form == ADV_FORM_COLLOCATION || h.cfg.fused_form == ADV_FORM_COLLOCATION_NO_TRACES)
     return true;
   return h.cfg.precision == ADV_PRECISION_FP64 || h.cfg.diffusion != 0.0;
+}
+
+// Face traces between the collocation stages: FP64 advection (SIPG needs
+// normal derivatives of the neighbours, the FP32 operator keeps its bytes)
+bool use_traces(const adv_handle &h)
+{
+  return h.cfg.precision == ADV_PRECISION_FP64 && h.cfg.diffusion == 0.0 &&
+         h.cfg.fused_form != ADV_FORM_COLLOCATION_NO_TRACES;
+}
+
+int ensure_traces(adv_handle *h)
+{
+  const size_t nb = (size_t)h->mesh.n_cells * 6 * h->mesh.n * h->mesh.n * sizeof(double);
+  for (int i = 0; i < 2; ++i)
+    if (!h->d_traces[i])
+      {
+        ADV_CUDA(cudaMalloc(&h->d_traces[i], nb));
+        h->device_bytes += nb;
+      }
+  return ADV_OK;
 }
 
 int ensure_scratch(adv_handle *h, int i)
@@ -551,6 +571,8 @@ int adv_destroy(adv_handle *h)
   cudaFree(h->d_fdm_cell_f);
   cudaFree(h->d_scratch[0]);
   cudaFree(h->d_scratch[1]);
+  cudaFree(h->d_traces[0]);
+  cudaFree(h->d_traces[1]);
   delete h;
   return ADV_OK;
 }
@@ -730,10 +752,16 @@ int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, 
     return fail(ADV_ERR_INVALID, "one-stage schemes are not supported");
   // collocation form: the solution moves to the Gauss-point values for the
   // steps and back afterwards (r and k are scratch either way)
-  const bool gauss = n_steps > 0 && use_collocation(*h);
+  const bool gauss  = n_steps > 0 && use_collocation(*h);
+  const bool traces = gauss && use_traces(*h);
+  if (traces)
+    if (int e = ensure_traces(h))
+      return e;
+  double *tr_in = h->d_traces[0], *tr_out = h->d_traces[1];
   if (gauss)
     {
-      ADV_CUDA(adv::launch_basis_change(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, true, s));
+      ADV_CUDA(adv::launch_basis_change(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, true, s,
+                                        traces ? tr_in : nullptr));
       ++h->launches;
     }
   for (int step = 0; step < n_steps; ++step)
@@ -752,6 +780,12 @@ int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, 
           const double   fac = A.out_scale;
           const bool     last = st == ns - 1;
           A.gauss             = gauss;
+          if (traces)
+            {
+              A.tr_in  = tr_in;
+              A.tr_out = tr_out;
+              std::swap(tr_in, tr_out);
+            }
           A.b                 = bi[st] * dt * fac;
           A.a                 = last ? 0.0 : ai[st] * dt * fac;
           A.mode              = last ? adv::kModeLastStage : adv::kModeStage;

@@ -164,20 +164,32 @@ __device__ __forceinline__ void sweep2(const T (&M)[kMaxNDev][kMaxNDev], const E
 // right-hand-side sign convention): dnlo / dnhi are the neighbour's reference
 // normal derivatives at the face points, blo / bhi mark Dirichlet faces
 // (mirror data u+ = 2g - u-, grad u+ = grad u-).
-template <int N, typename T, bool UNI, bool VISC, int D>
-__device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTables<T> &tb,
-                                               const T (&U)[N], T nlo, T nhi, T dnlo, T dnhi, bool blo,
-                                               bool bhi, int fq, const T *Flo, const T *Fhi, const T *vt,
-                                               int vstride, T (&out)[N])
+// The own face values of the pencil: ulo = sum_q l_q(0) U_q, uhi = sum_q l_q(1) U_q.
+template <int N, typename T>
+__device__ __forceinline__ void pencil_traces(const DevTables<T> &tb, const T (&U)[N], T &ulo, T &uhi)
 {
-  constexpr int NF = N * N;
-  T             ulo = tb.l0[0] * U[0], uhi = tb.l1[0] * U[0];
+  ulo = tb.l0[0] * U[0], uhi = tb.l1[0] * U[0];
 #pragma unroll
   for (int q = 1; q < N; ++q)
     {
       ulo = fma(tb.l0[q], U[q], ulo);
       uhi = fma(tb.l1[q], U[q], uhi);
     }
+}
+
+// OWN_TR: the own face values come precomputed (tr_lo, tr_hi)
+template <int N, typename T, bool UNI, bool VISC, int D, bool OWN_TR = false>
+__device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTables<T> &tb,
+                                               const T (&U)[N], T nlo, T nhi, T dnlo, T dnhi, bool blo,
+                                               bool bhi, int fq, const T *Flo, const T *Fhi, const T *vt,
+                                               int vstride, T (&out)[N], T tr_lo = T(0), T tr_hi = T(0))
+{
+  constexpr int NF = N * N;
+  T             ulo, uhi;
+  if (OWN_TR)
+    ulo = tr_lo, uhi = tr_hi;
+  else
+    pencil_traces<N, T>(tb, U, ulo, uhi);
   T Plo, Mlo, Phi, Mhi;
   if (UNI)
     {

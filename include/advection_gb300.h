@@ -65,6 +65,9 @@ enum { ADV_LSRK_3_3 = 0, ADV_LSRK_5_4 = 1, ADV_LSRK_7_4 = 2, ADV_LSRK_9_5 = 3 };
 #define ADV_FORM_AUTO 0
 #define ADV_FORM_NODAL 1
 #define ADV_FORM_COLLOCATION 2
+/* collocation without the face traces that FP64 advection stages pass to the
+ * next stage (same results bit for bit; for comparisons) */
+#define ADV_FORM_COLLOCATION_NO_TRACES 3
 
 typedef struct adv_config
 {

@@ -142,8 +142,9 @@ def test_lsrk_steps_match_oracle(cuda, oracle_mod, adv_lib, case, scheme):
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_collocation_form_of_fused_steps(cuda, oracle_mod, adv_lib, case, precision):
-    """The fused step loop in the Gauss-point (collocation) basis and in the
-    nodal basis, both against the oracle's stage loop."""
+    """The fused step loop in the Gauss-point (collocation) basis, with and
+    without face traces between the stages, and in the nodal basis, against
+    the oracle's stage loop."""
     torch = cuda
     cfg = CASES[case]
     o = oracle_mod.Oracle(**cfg)
@@ -153,14 +154,14 @@ def test_collocation_form_of_fused_steps(cuda, oracle_mod, adv_lib, case, precis
     for s in range(4):
         o.lsrk_step(0.05 + s * dt, dt, u, r, k)
     res = {}
-    for form in (adv_lib.FORM_NODAL, adv_lib.FORM_COLLOCATION):
+    for form in (adv_lib.FORM_NODAL, adv_lib.FORM_COLLOCATION, adv_lib.FORM_COLLOCATION_NO_TRACES):
         g = adv_lib.AdvectionOperation(**cfg, precision=precision, fused_form=form)
         ud = g.initialize_dof_vector()
         g.project_initial(ud)
         rd, kd = g.initialize_dof_vector(), g.initialize_dof_vector()
         n0 = g.launch_count()
         g.lsrk_steps(adv_lib.LSRK_5_4, 0.05, dt, 4, ud, rd, kd)
-        assert g.launch_count() - n0 == 20 + (2 if form == adv_lib.FORM_COLLOCATION else 0)
+        assert g.launch_count() - n0 == 20 + (0 if form == adv_lib.FORM_NODAL else 2)
         res[form] = ud.cpu().numpy()
         g.lsrk_steps(adv_lib.LSRK_5_4, 0.05, dt, 0, ud, rd, kd)  # no steps: no change of basis either
         assert np.array_equal(ud.cpu().numpy(), res[form])
@@ -169,6 +170,8 @@ def test_collocation_form_of_fused_steps(cuda, oracle_mod, adv_lib, case, precis
     assert rel_err(res[adv_lib.FORM_NODAL], u) <= tol
     if precision == 0:
         assert rel_err(res[adv_lib.FORM_COLLOCATION], res[adv_lib.FORM_NODAL]) <= 1e-13
+    # face traces passed between the stages change no bit
+    np.testing.assert_array_equal(res[adv_lib.FORM_COLLOCATION], res[adv_lib.FORM_COLLOCATION_NO_TRACES])
 
 
 def test_integrator_stage_loop_equals_fused_step(cuda, adv_lib):
