@@ -195,10 +195,12 @@ def run_mix(requests, rate_clock=True, memory_budget_bytes=150 * 10 ** 9, steps_
     return results, summary, sols
 
 
-def run_one_at_a_time(requests):
-    """Baseline: the requests one after another, each through its own
-    AdvectionOperation and the fused LSRK step loop, in arrival order (no
-    arrival clock).  Returns (results, summary)."""
+def run_one_at_a_time(requests, rate_clock=True):
+    """Baseline: a single worker serving the requests one after another in
+    arrival order, each through its own AdvectionOperation and the fused LSRK
+    step loop; a request waits for its arrival time (with rate_clock) and for
+    the requests before it.  Latency = completion - arrival, as for the
+    server.  Returns (results, summary)."""
     import torch
 
     from . import AdvectionOperation, LSRK_5_4
@@ -206,7 +208,10 @@ def run_one_at_a_time(requests):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for r in sorted(requests, key=lambda q: q.arrival):
-        ts = time.perf_counter()
+        arrival = r.arrival if rate_clock else 0.0
+        wait = arrival - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
         op = AdvectionOperation(r.config())
         steps = r.steps()
         dt = r.t_end / steps
@@ -214,13 +219,15 @@ def run_one_at_a_time(requests):
         op.project_initial(u)
         op.lsrk_steps(LSRK_5_4, 0.0, dt, steps, u, rr, k)
         err, nrm = op.l2_error(u, r.t_end)
-        results[r.index] = {"rel_l2_error": err / nrm, "latency_s": time.perf_counter() - ts, "steps": steps,
-                            "dt": dt}
+        results[r.index] = {"rel_l2_error": err / nrm, "latency_s": time.perf_counter() - t0 - arrival,
+                            "steps": steps, "dt": dt}
         op.close()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     work = sum(r.work() for r in requests)
+    lat = np.array([results[r.index]["latency_s"] for r in requests])
     summary = {"requests": len(requests), "wall_s": wall, "throughput_req_s": len(requests) / wall,
+               "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
                "gdof_stages_per_s": work / wall / 1e9}
     return results, summary
 
@@ -240,7 +247,7 @@ def main(argv=None):
                             steps_per_tick=args.steps_per_tick)
     out = {"rate_req_s": args.rate, "seed": args.seed, "t_range": [0.1, args.t_max], "serving": summary}
     if args.baseline:
-        _, base = run_one_at_a_time(reqs)
+        _, base = run_one_at_a_time(reqs, rate_clock=bool(args.rate))
         out["one_at_a_time"] = base
     print(json.dumps(out))
 
