@@ -21,6 +21,11 @@ namespace
 template <typename T>
 constexpr bool kBatchCollocation = sizeof(T) == sizeof(double);
 
+// dynamic shared memory of the per-CTA code the group runs
+template <int N, typename T>
+constexpr int kBatchSmem = kBatchCollocation<T> ? GaussShape<N, T, true, false, true>::SMEM
+                                                : StageShape<N, T, true, false>::SMEM;
+
 template <int N, typename T>
 __global__ void __launch_bounds__(StageShape<N, T, true, false>::THREADS) batch_stage_kernel(const BatchLaunch L)
 {
@@ -67,6 +72,14 @@ __global__ void __launch_bounds__(StageShape<N, T, true, false>::THREADS) batch_
           a.b    = L.bi[st] * S.dt;
           a.a    = last ? 0.0 : L.ai[st] * S.dt;
           a.mode = last ? kModeLastStage : kModeStage;
+          if (kBatchCollocation<T>)
+            {
+              // stage count of the solve so far: even reads t0, odd reads t1
+              // (the single-mesh loop alternates the same way from t0)
+              const bool odd = ((S.steps_done * L.n_stages + st) & 1) != 0;
+              a.tr_in        = odd ? S.t1 : S.t0;
+              a.tr_out       = odd ? S.t0 : S.t1;
+            }
           sA     = a;
         }
     }
@@ -74,7 +87,7 @@ __global__ void __launch_bounds__(StageShape<N, T, true, false>::THREADS) batch_
   if (skip)
     return;
   if constexpr (kBatchCollocation<T>)
-    stage_gauss_cta<N, T, true, false>(sA, cell0, smem_raw);
+    stage_gauss_cta<N, T, true, false, true>(sA, cell0, smem_raw);
   else
     stage_cta<N, T, true, false>(sA, cell0, smem_raw);
 }
@@ -90,14 +103,14 @@ template <int N, typename T>
 cudaError_t prepare_batch_t()
 {
   return cudaFuncSetAttribute(batch_stage_kernel<N, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              StageShape<N, T, true, false>::SMEM);
+                              kBatchSmem<N, T>);
 }
 
 template <int N, typename T>
 cudaError_t launch_batch_t(const BatchLaunch &L, int cta_capacity, cudaStream_t s)
 {
   using SH = StageShape<N, T, true, false>;
-  batch_stage_kernel<N, T><<<cta_capacity, SH::THREADS, SH::SMEM, s>>>(L);
+  batch_stage_kernel<N, T><<<cta_capacity, SH::THREADS, kBatchSmem<N, T>, s>>>(L);
   return cudaGetLastError();
 }
 } // namespace

@@ -11,6 +11,7 @@ namespace adv
 struct BatchSlot
 {
   double   *u, *r, *k;      // solution and the two Runge-Kutta registers
+  double   *t0, *t1;        // collocation form: face traces of the stage inputs (even / odd stage count)
   int       n;              // cells per direction of the periodic unit cube
   int       steps_total;    // time steps of the solve
   int       steps_done;     // advanced by the step-advance kernel

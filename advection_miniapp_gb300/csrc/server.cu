@@ -48,6 +48,7 @@ struct SReq
   double              dt = 0;
   int                 steps = 0, steps_done = 0;
   double             *u = nullptr, *r = nullptr, *k = nullptr;
+  double             *t0 = nullptr, *t1 = nullptr; // face traces (collocation groups)
   int                 state = 0; // 0 queued, 1 active, 2 done, 3 failed
   double              t_submit = 0, t_admit = 0, t_done = 0, rel_l2 = -1;
   std::vector<double> solution;
@@ -194,6 +195,7 @@ int rebuild(adv_server *S, SGroup &g)
       adv::BatchSlot &b = slots[i];
       std::memset(&b, 0, sizeof(b));
       b.u = q.u, b.r = q.r, b.k = q.k;
+      b.t0 = q.t0, b.t1 = q.t1;
       b.n           = q.n;
       b.steps_total = q.steps;
       b.steps_done  = q.steps_done;
@@ -253,7 +255,12 @@ int retire(adv_server *S, SGroup &g, int64_t id)
   ADV_CUDA(cudaFreeAsync(q.u, g.stream));
   ADV_CUDA(cudaFreeAsync(q.r, g.stream));
   ADV_CUDA(cudaFreeAsync(q.k, g.stream));
-  q.u = q.r = q.k = nullptr;
+  if (q.t0)
+    {
+      ADV_CUDA(cudaFreeAsync(q.t0, g.stream));
+      ADV_CUDA(cudaFreeAsync(q.t1, g.stream));
+    }
+  q.u = q.r = q.k = q.t0 = q.t1 = nullptr;
   q.state  = 2;
   q.t_done = now_s();
   S->used -= q.bytes;
@@ -278,7 +285,10 @@ int admit(adv_server *S, int64_t id)
   if (adv::batch_collocation(q.precision))
     {
       const long long cells = (long long)q.n * q.n * q.n;
-      ADV_CUDA(adv::launch_basis_change(q.npts, q.u, 0, cells, true, g->stream));
+      const size_t    tb    = (size_t)cells * 6 * q.npts * q.npts * sizeof(double);
+      ADV_CUDA(cudaMallocAsync((void **)&q.t0, tb, g->stream));
+      ADV_CUDA(cudaMallocAsync((void **)&q.t1, tb, g->stream));
+      ADV_CUDA(adv::launch_basis_change(q.npts, q.u, 0, cells, true, g->stream, q.t0));
       ++S->launches;
     }
   q.state   = 1;
@@ -323,6 +333,8 @@ int adv_server_destroy(adv_server *S)
       cudaFree(q.u);
       cudaFree(q.r);
       cudaFree(q.k);
+      cudaFree(q.t0);
+      cudaFree(q.t1);
     }
   for (auto &kv : S->groups)
     {
@@ -372,6 +384,8 @@ int adv_server_submit(adv_server *S, const adv_config *cfg, double t_end, double
   q.precision = c.precision;
   q.n_dofs    = (int64_t)q.n * q.n * q.n * q.npts * q.npts * q.npts;
   q.bytes     = 3 * q.n_dofs * (int64_t)sizeof(double);
+  if (adv::batch_collocation(q.precision)) // two face-trace buffers of 6 n^2 values per cell
+    q.bytes += 2 * 6 * (q.n_dofs / q.npts) * (int64_t)sizeof(double);
   adv::Mesh m;
   adv::setup_mesh(c, m);
   adv::Tables1D tb;

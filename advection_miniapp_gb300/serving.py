@@ -53,6 +53,15 @@ class Request:
         dt = self.courant * (1.0 / self.n) / np.linalg.norm(self.velocity) / self.degree ** 1.5
         return max(1, int(np.ceil(self.t_end / dt - 1e-12)))
 
+    def device_bytes(self):
+        """Device memory the server reserves for the solve: u, r, k and, for
+        the FP64 operator (collocation form), two face-trace buffers of
+        6 (k+1)^2 values per cell."""
+        b = 3 * 8 * self.n_dofs
+        if self.precision == PRECISION_FP64:
+            b += 2 * 6 * 8 * self.n_dofs // (self.degree + 1)
+        return b
+
     def work(self):
         """DoF-stages of the solve (5 stages per step)."""
         return self.n_dofs * 5 * self.steps()

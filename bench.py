@@ -75,7 +75,7 @@ def _sweep_cost(n, anti):
     return inst, flops
 
 
-def fp_work_per_cell(n, curved=True, stage=True, collocation=False):
+def fp_work_per_cell(n, curved=True, stage=True, collocation=False, traces=False):
     """(FP instructions, flops with FMA = 2) of one fused stage per cell,
     phase by phase as in the kernels.  Nodal form (stage_kernel.cuh):
     interpolation sweeps of the own cell (3 x n^2 pencils) and of the six
@@ -84,18 +84,24 @@ def fp_work_per_cell(n, curved=True, stage=True, collocation=False):
     1/det J, three inverse-mass sweeps and the two-FMA update per DoF.
     Collocation form (stage_gauss.cuh): no interpolation or inverse-mass
     sweeps; the neighbours' face values are n-term contractions at the 6 n^2
-    face points."""
+    face points.  With face traces the stage reads its own and the
+    neighbours' face values and instead contracts the 3 n^2 pencils of its
+    output (2n FMAs each) for the next stage."""
     si, sf = _sweep_cost(n, anti=False)
     di, df = _sweep_cost(n, anti=True)
     p = n * n
-    if collocation:
+    if collocation and traces:
+        inst = 3 * p * 2 * n
+        flops = 3 * p * 2 * (2 * n - 1)
+    elif collocation:
         inst = 6 * p * n
         flops = 6 * p * (2 * n - 1)
     else:
         inst = 3 * p * si + 12 * n * si
         flops = 3 * p * sf + 12 * n * sf
-    pass_i = 2 * n + 4 + (n if curved else n) + di + 2 * n
-    pass_f = 2 * (2 * n - 1) + 6 + n + df + 4 * n
+    own_i, own_f = (0, 0) if traces else (2 * n, 2 * (2 * n - 1))
+    pass_i = own_i + 4 + n + di + 2 * n
+    pass_f = own_f + 6 + n + df + 4 * n
     inst += 3 * p * pass_i
     flops += 3 * p * pass_f
     if curved:
@@ -372,10 +378,10 @@ def ours(args):
     launch32 = r32["seconds"] / (STAGES * args.steps)
     # average over the 5 launches of a step: 4 stages with 2 update FMAs per DoF, the last with 1;
     # FP64 runs the collocation form, FP32 the nodal form (the library's default choice)
-    inst = (4 * fp_work_per_cell(n, collocation=True)[0]
-            + fp_work_per_cell(n, stage=False, collocation=True)[0]) / STAGES
-    flops = (4 * fp_work_per_cell(n, collocation=True)[1]
-             + fp_work_per_cell(n, stage=False, collocation=True)[1]) / STAGES
+    inst = (4 * fp_work_per_cell(n, collocation=True, traces=True)[0]
+            + fp_work_per_cell(n, stage=False, collocation=True, traces=True)[0]) / STAGES
+    flops = (4 * fp_work_per_cell(n, collocation=True, traces=True)[1]
+             + fp_work_per_cell(n, stage=False, collocation=True, traces=True)[1]) / STAGES
     flops32 = (4 * fp_work_per_cell(n)[1] + fp_work_per_cell(n, stage=False)[1]) / STAGES
     vec_bytes_launch = bytes_per_dof_step() / STAGES * n_dofs
     # FP64 instructions of any kind (FMA, add, mul) take one issue slot of the
@@ -418,7 +424,7 @@ def ours(args):
         "roofline": {"bound": "fp64", "achieved": round(achieved64, 4), "peak": round(fp64_peak, 4),
                      "unit": "TFLOP/s", "frac": round(achieved64 / fp64_peak, 4),
                      "traffic": traffic(NCU_TRAFFIC_PER_DOF["fp64"], n_dofs),
-                     "form": "collocation (Gauss-point values inside lsrk_steps)",
+                     "form": "collocation with face traces (Gauss-point values inside lsrk_steps)",
                      "peak_source": "FP64 FMA microbenchmark (adv_measure_fma_peak) on this GPU",
                      "achieved_definition": "2 x FP64 instructions per second (each FP64 add/mul/FMA takes one "
                                             "FMA issue slot); algorithmic_tflops counts FMA = 2, add/mul = 1",

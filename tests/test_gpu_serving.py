@@ -59,7 +59,7 @@ def test_fp64_request_matches_oracle(cuda, oracle_mod):
 def test_budget_limits_concurrency(cuda, adv_lib):
     from advection_miniapp_gb300.serving import Server
     reqs = small_mix(seed=5, n=10)
-    biggest = max(3 * 8 * r.n_dofs for r in reqs)
+    biggest = max(r.device_bytes() for r in reqs)
     budget = 2 * biggest
     with Server(memory_budget_bytes=budget, steps_per_tick=2, keep_solutions=True) as srv:
         ids = [srv.submit(r) for r in reqs]
@@ -70,6 +70,7 @@ def test_budget_limits_concurrency(cuda, adv_lib):
             peak_bytes = max(peak_bytes, st["device_bytes"])
             peak_running = max(peak_running, st["running"])
         assert peak_bytes <= budget
+        assert srv.stats()["device_bytes"] == 0
         assert 1 <= peak_running < len(reqs)
         limited = [srv.solution(i, r.n_dofs) for i, r in zip(ids, reqs)]
     with Server(keep_solutions=True, max_active=3) as srv:
@@ -84,7 +85,7 @@ def test_budget_limits_concurrency(cuda, adv_lib):
 def test_rejected_requests(cuda, adv_lib):
     from advection_miniapp_gb300.serving import Request, Server
     r = Request(0, 4, 3, (1.0, 0.0, 0.0), (0.0, 0.0, 0.0), 0.1, 0)
-    with Server(memory_budget_bytes=3 * 8 * r.n_dofs - 1) as srv:
+    with Server(memory_budget_bytes=r.device_bytes() - 1) as srv:
         with pytest.raises(adv_lib.AdvError):
             srv.submit(r)
     with Server() as srv:

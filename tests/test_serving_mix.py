@@ -37,3 +37,11 @@ def test_step_rule():
         s = r.steps()
         assert r.t_end / s <= dt0 * (1 + 1e-12)
         assert s == 1 or r.t_end / (s - 1) > dt0 * (1 - 1e-12)
+
+
+def test_device_bytes_of_a_request():
+    from advection_miniapp_gb300.serving import Request
+    r64 = Request(0, 4, 3, (1.0, 0.0, 0.0), (0.0, 0.0, 0.0), 0.1, 0)
+    r32 = Request(1, 4, 3, (1.0, 0.0, 0.0), (0.0, 0.0, 0.0), 0.1, 1)
+    assert r32.device_bytes() == 3 * 8 * 64 * 64
+    assert r64.device_bytes() == 3 * 8 * 64 * 64 + 2 * 6 * 16 * 8 * 64
