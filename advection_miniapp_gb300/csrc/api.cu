@@ -117,6 +117,14 @@ int ensure_tables(int device)
           tf[n].lwd0[q] = (float)t.lwd0[q], tf[n].lwd1[q] = (float)t.lwd1[q];
           tf[n].dphi0[q] = (float)t.dphi0[q], tf[n].dphi1[q] = (float)t.dphi1[q];
         }
+      for (int q = 0; q < n / 2; ++q)
+        {
+          const double e = 0.5 * (t.lw0[q] + t.lw0[n - 1 - q]), o = 0.5 * (t.lw0[q] - t.lw0[n - 1 - q]);
+          td[n].lwe[q] = e, td[n].lwo[q] = o;
+          tf[n].lwe[q] = (float)e, tf[n].lwo[q] = (float)o;
+        }
+      if (n % 2)
+        td[n].lwe[n / 2] = t.lw0[n / 2], tf[n].lwe[n / 2] = (float)t.lw0[n / 2];
       double Si[adv::kMaxN][adv::kMaxN] = {};
       for (int i = 0; i < n; ++i)
         for (int q = 0; q < n; ++q)
@@ -361,17 +369,17 @@ bool use_collocation(const adv_handle &h)
   return h.cfg.precision == ADV_PRECISION_FP64 || h.cfg.diffusion != 0.0;
 }
 
-// Face traces between the collocation stages: FP64 advection (SIPG needs
-// normal derivatives of the neighbours, the FP32 operator keeps its bytes)
+// Face traces between the collocation stages of advection (SIPG needs normal
+// derivatives of the neighbours)
 bool use_traces(const adv_handle &h)
 {
-  return h.cfg.precision == ADV_PRECISION_FP64 && h.cfg.diffusion == 0.0 &&
-         h.cfg.fused_form != ADV_FORM_COLLOCATION_NO_TRACES;
+  return h.cfg.diffusion == 0.0 && h.cfg.fused_form != ADV_FORM_COLLOCATION_NO_TRACES;
 }
 
 int ensure_traces(adv_handle *h)
 {
-  const size_t nb = (size_t)h->mesh.n_cells * 6 * h->mesh.n * h->mesh.n * sizeof(double);
+  const size_t word = h->cfg.precision == ADV_PRECISION_FP64 ? sizeof(double) : sizeof(float);
+  const size_t nb   = (size_t)h->mesh.n_cells * 6 * h->mesh.n * h->mesh.n * word;
   for (int i = 0; i < 2; ++i)
     if (!h->d_traces[i])
       {
@@ -757,11 +765,11 @@ int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, 
   if (traces)
     if (int e = ensure_traces(h))
       return e;
-  double *tr_in = h->d_traces[0], *tr_out = h->d_traces[1];
+  void *tr_in = h->d_traces[0], *tr_out = h->d_traces[1];
   if (gauss)
     {
       ADV_CUDA(adv::launch_basis_change(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, true, s,
-                                        traces ? tr_in : nullptr));
+                                        traces ? tr_in : nullptr, h->cfg.precision != ADV_PRECISION_FP64));
       ++h->launches;
     }
   for (int step = 0; step < n_steps; ++step)

@@ -42,6 +42,10 @@ struct DevTables
   // viscous (SIPG) terms: Gauss-Lagrange derivatives at the faces, the same
   // divided by the weights, nodal-basis derivatives at the faces
   T ld0[kMaxNDev], ld1[kMaxNDev], lwd0[kMaxNDev], lwd1[kMaxNDev], dphi0[kMaxNDev], dphi1[kMaxNDev];
+  // lift vectors split by the mirror symmetry lw1[q] = lw0[n-1-q]:
+  // lwe[q] = (lw0[q] + lw0[n-1-q]) / 2, lwo[q] = (lw0[q] - lw0[n-1-q]) / 2
+  // for q < n/2, lwe[n/2] = lw0[n/2] for odd n
+  T lwe[kMaxNDev], lwo[kMaxNDev];
 };
 
 // Index [n] holds the tables of n points per direction.  The library is

@@ -26,7 +26,7 @@ struct adv_handle
   double  *d_face_x[3]   = {};
   double  *d_partials    = nullptr;
   double  *d_scratch[2]  = {};
-  double  *d_traces[2]   = {}; // face traces of the collocation step loop (lazily allocated)
+  void    *d_traces[2]   = {}; // face traces of the collocation step loop (lazily allocated)
   int64_t  device_bytes  = 0;
   int64_t  launches      = 0;
   adv::DiagArgs diag;

@@ -20,10 +20,11 @@
 // The fused LSRK loop changes the basis of the solution once on entry and
 // once on exit (launch_basis_change); the stages in between run here.
 //
-// Face traces (TR, FP64 advection): a stage also writes the values at the
-// face points of its output that the next stage reads (r_out, or u_out on a
-// last stage), [6][n^2] per cell; the next stage then reads its own and its
-// neighbours' face values instead of contracting pencils.  Per cell-stage at
+// Face traces (TR, advection): a stage also writes the values at the face
+// points of its output that the next stage reads (r_out, or u_out on a last
+// stage), [6][n^2] per cell in the operator's precision; the next stage then
+// reads its own and its neighbours' face values instead of contracting
+// pencils.  Per cell-stage at
 // degree 4 the producer adds 750 FMAs and the consumer saves 1500; the
 // traces are the same contractions in the same order, so results are
 // bit-identical to the variant without them.
@@ -80,9 +81,9 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
       Ub[i] = from_double<T>(__ldg(src + i));
     if (TR)
       {
-        const double *tr = A.tr_in + cell0 * 6 * NF;
+        const T *tr = static_cast<const T *>(A.tr_in) + cell0 * 6 * NF;
         for (int i = tid; i < ncell * 6 * NF; i += NT)
-          Tb[i] = from_double<T>(__ldg(tr + i));
+          Tb[i] = __ldg(tr + i);
       }
   }
   for (int w = tid; w < ncell * 6 * NF; w += NT)
@@ -95,7 +96,7 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
           if (TR)
             {
               // the neighbour's own trace on the shared face (its face j ^ 1)
-              Nb[cf * NF + fq] = from_double<T>(__ldg(A.tr_in + ((long long)nb * 6 + (j ^ 1)) * NF + fq));
+              Nb[cf * NF + fq] = __ldg(static_cast<const T *>(A.tr_in) + ((long long)nb * 6 + (j ^ 1)) * NF + fq);
               continue;
             }
           // pencil of the neighbour along d through face point fq, contracted
@@ -238,16 +239,21 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
         }
       if (TR)
         {
-          // z traces from registers; the pencil goes to this thread's own
-          // column of Qb (read above by this thread only) for the x and y traces
-          double lo, hi;
-          pencil_traces<N, double>(tab<double>(N), next, lo, hi);
-          double *to = A.tr_out + (cell0 + cl) * 6 * NF + r;
+          // the next input in the operator's precision (what the next stage
+          // would load); z traces from registers, and the pencil goes to this
+          // thread's own column of Qb (read above by this thread only) for
+          // the x and y traces
+          T nt[N], lo, hi;
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            nt[k] = from_double<T>(next[k]);
+          pencil_traces<N, T>(tb, nt, lo, hi);
+          T *to      = static_cast<T *>(A.tr_out) + (cell0 + cl) * 6 * NF + r;
           to[4 * NF] = lo;
           to[5 * NF] = hi;
 #pragma unroll
           for (int k = 0; k < N; ++k)
-            z[k * NF] = next[k];
+            z[k * NF] = nt[k];
         }
     }
   if (TR)
@@ -255,19 +261,19 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
       __syncthreads();
       for (int w = tid; w < 2 * ncell * NF; w += NT)
         {
-          const int    dd = w / (ncell * NF), v = w % (ncell * NF);
-          const int    cl = v / NF, r = v % NF;
-          const int    off = dd == 0 ? N * r : (r % N) + NF * (r / N);
-          const int    st  = dd == 0 ? 1 : N;
-          const double *p  = reinterpret_cast<const double *>(Qb) + cl * NQ + off;
-          double        x[N], lo, hi;
+          const int dd = w / (ncell * NF), v = w % (ncell * NF);
+          const int cl = v / NF, r = v % NF;
+          const int off = dd == 0 ? N * r : (r % N) + NF * (r / N);
+          const int st  = dd == 0 ? 1 : N;
+          const T  *p   = Qb + cl * NQ + off;
+          T         x[N], lo, hi;
 #pragma unroll
           for (int k = 0; k < N; ++k)
             x[k] = p[k * st];
-          pencil_traces<N, double>(tab<double>(N), x, lo, hi);
-          double *to = A.tr_out + ((cell0 + cl) * 6 + 2 * dd) * NF + r;
-          to[0]      = lo;
-          to[NF]     = hi;
+          pencil_traces<N, T>(tb, x, lo, hi);
+          T *to  = static_cast<T *>(A.tr_out) + ((cell0 + cl) * 6 + 2 * dd) * NF + r;
+          to[0]  = lo;
+          to[NF] = hi;
         }
     }
 }
@@ -308,10 +314,9 @@ cudaError_t launch_stage_gauss_n(const StageArgs &args, cudaStream_t stream)
 {
   if (args.visc)
     return launch_stage_gauss_t<N, T, false, true, false>(args, stream);
-  if constexpr (sizeof(T) == sizeof(double))
-    if (args.tr_in)
-      return args.uniform ? launch_stage_gauss_t<N, T, true, false, true>(args, stream)
-                          : launch_stage_gauss_t<N, T, false, false, true>(args, stream);
+  if (args.tr_in)
+    return args.uniform ? launch_stage_gauss_t<N, T, true, false, true>(args, stream)
+                        : launch_stage_gauss_t<N, T, false, false, true>(args, stream);
   return args.uniform ? launch_stage_gauss_t<N, T, true, false, false>(args, stream)
                       : launch_stage_gauss_t<N, T, false, false, false>(args, stream);
 }

@@ -145,6 +145,51 @@ __device__ __forceinline__ void sweep_eo(const EvenOdd<T> &M, const T (&in)[N], 
     }
 }
 
+// out = Dw-type (antisymmetric) even-odd product of `in` plus the lifted face
+// fluxes lw0 phlo + lw1 phhi, folded into the recombination of the even and
+// odd halves: with ps = phlo + phhi, pd = phlo - phhi, the lift of point q is
+// lwe[q] ps + lwo[q] pd and of point n-1-q lwe[q] ps - lwo[q] pd, so the
+// pair costs two FMAs instead of four.
+template <int N, typename T>
+__device__ __forceinline__ void sweep_eo_anti_lift(const EvenOdd<T> &M, const T (&in)[N], T phlo, T phhi,
+                                                   const T *lwe, const T *lwo, T (&out)[N])
+{
+  constexpr int H = N / 2;
+  T             e[H], o[H];
+#pragma unroll
+  for (int i = 0; i < H; ++i)
+    {
+      e[i] = in[i] + in[N - 1 - i];
+      o[i] = in[i] - in[N - 1 - i];
+    }
+  const T ps = phlo + phhi, pd = phlo - phhi;
+#pragma unroll
+  for (int q = 0; q < H; ++q)
+    {
+      T E = M.e[q][0] * e[0], O = M.o[q][0] * o[0];
+#pragma unroll
+      for (int i = 1; i < H; ++i)
+        {
+          E = fma(M.e[q][i], e[i], E);
+          O = fma(M.o[q][i], o[i], O);
+        }
+      if (N % 2)
+        E = fma(M.ce[q], in[H], E);
+      const T a      = fma(lwe[q], ps, O);
+      const T b      = fma(lwo[q], pd, E);
+      out[q]         = a + b;
+      out[N - 1 - q] = a - b;
+    }
+  if (N % 2)
+    {
+      T m = M.mid[0] * o[0];
+#pragma unroll
+      for (int i = 1; i < H; ++i)
+        m = fma(M.mid[i], o[i], m);
+      out[H] = fma(lwe[H], ps, m);
+    }
+}
+
 // Sweep with the cheaper of the two forms: even-odd pays off from n = 5.
 template <int N, typename T, bool ANTI>
 __device__ __forceinline__ void sweep2(const T (&M)[kMaxNDev][kMaxNDev], const EvenOdd<T> &Meo,
@@ -231,6 +276,29 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
     }
   // volume term: (1 - skew) (a u, grad v) - skew (a . grad u, v) - nu (grad u, grad v)
   // (advection_solver.cc:500-507); with vt = det J J^{-1} a per Gauss point
+  if constexpr (!VISC && N >= 5)
+    {
+      // (1 - skew) Dw (c U) + lifts - skew c D U with c = a_d / h_d (uniform)
+      // or vt (field); the lifts ride on the even-odd recombination
+      const T cvd = Consts<T>::cv(A, D);
+      const T sk  = A.has_skew ? Consts<T>::skew(A) : T(0);
+      T       w[N], du[N];
+#pragma unroll
+      for (int q = 0; q < N; ++q)
+        {
+          const T c = UNI ? cvd : vt[q * vstride];
+          w[q]      = A.has_skew ? (T(1) - sk) * (c * U[q]) : c * U[q];
+        }
+      sweep_eo_anti_lift<N, T>(tb.Dw_eo, w, phlo, phhi, tb.lwe, tb.lwo, out);
+      if (A.has_skew)
+        {
+          sweep2<N, T, true>(tb.D, tb.D_eo, U, du);
+#pragma unroll
+          for (int q = 0; q < N; ++q)
+            out[q] = fma(-sk * (UNI ? cvd : vt[q * vstride]), du[q], out[q]);
+        }
+      return;
+    }
   T vtv[N], w[N], du[N];
   const bool need_du = VISC || A.has_skew;
   if (need_du)
