@@ -37,11 +37,16 @@ namespace adv
 template <int N, typename T, bool UNI, bool VISC, bool TR>
 struct GaussShape
 {
-  using SH                    = StageShape<N, T, UNI, VISC>;
-  static constexpr int C      = SH::C;
+  using SH                     = StageShape<N, T, UNI, VISC>;
+  static constexpr int C       = SH::C;
   static constexpr int THREADS = SH::THREADS;
-  // the nodal layout plus, with traces, Tb [C][6][NF] own face values
-  static constexpr int SMEM = SH::SMEM + (TR ? 6 * C * N * N * (int)sizeof(T) : 0);
+  // the nodal layout plus, with traces, Tb [C][6][NF] own face values,
+  // padded to 16 bytes: the geometry after it is filled by 16-byte cp.async
+  static constexpr int TB_VALUES = TR ? (6 * C * N * N * (int)sizeof(T) + 15) / 16 * 16 / (int)sizeof(T) : 0;
+  static constexpr int SMEM      = SH::SMEM + TB_VALUES * (int)sizeof(T);
+  // byte offset of the cell geometry Gb in the layout of stage_gauss_cta
+  static constexpr int GB_OFFSET = (2 * C * N * N * N + 6 * C * N * N + TB_VALUES) * (int)sizeof(T);
+  static_assert(GB_OFFSET % 16 == 0, "cp.async destinations need 16-byte alignment");
 };
 
 template <int N, typename T, bool UNI, bool VISC, bool TR = false>
@@ -58,7 +63,7 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
   T   *Qb     = Ub + C * NQ;                     // [C][NQ] x and y contributions to Z
   T   *Nb     = Qb + C * NQ;                     // [C][6][NF] neighbour values at the face points
   T   *Tb     = Nb + C * 6 * NF;                 // traces: [C][6][NF] own values at the face points
-  T   *Gb     = Tb + (TR ? C * 6 * NF : 0);      // field: [C][4][NQ] cell geometry
+  T   *Gb     = Tb + GaussShape<N, T, UNI, VISC, TR>::TB_VALUES; // field: [C][4][NQ] cell geometry
   T   *Fb     = Gb + (UNI ? 0 : C * 4 * NQ);     // field: [C][6][2][NF] face coefficients
   T   *Nd     = Fb + (UNI ? 0 : C * 12 * NF);    // viscous: [C][6][NF] neighbour normal derivatives
   int *s_nbr  = reinterpret_cast<int *>(Nd + (VISC ? C * 6 * NF : 0));

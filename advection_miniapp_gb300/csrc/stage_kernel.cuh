@@ -50,6 +50,8 @@ struct StageShape
   static constexpr int VALUES =
     2 * C * NQ + 6 * C * NF + (UNI ? 0 : 4 * C * NQ + 12 * C * NF) + (VISC ? 6 * C * NF : 0);
   static constexpr int SMEM   = VALUES * (int)sizeof(T) + 12 * C * (int)sizeof(int);
+  // the cell geometry Gb (after Ub, Qb, Nb) is filled by 16-byte cp.async
+  static_assert((2 * C * NQ + 6 * C * NF) * (int)sizeof(T) % 16 == 0, "cp.async destinations need 16-byte alignment");
 };
 
 // index of the point with coordinate a along direction d and (b, c) along
