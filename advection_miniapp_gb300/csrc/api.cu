@@ -369,17 +369,20 @@ bool use_collocation(const adv_handle &h)
   return h.cfg.precision == ADV_PRECISION_FP64 || h.cfg.diffusion != 0.0;
 }
 
-// Face traces between the collocation stages of advection (SIPG needs normal
-// derivatives of the neighbours)
+// Face traces between the collocation stages: FP64 advection (SIPG needs
+// normal derivatives of the neighbours).  Measured on GB300 at degree 4, 64^3
+// curved cells: FP64 13.4 vs 12.3 GDoF/s without; the FP32 operator got
+// slower with them (54.3 vs 61.0: one more barrier, more shared memory per
+// CTA), so it does not use them.
 bool use_traces(const adv_handle &h)
 {
-  return h.cfg.diffusion == 0.0 && h.cfg.fused_form != ADV_FORM_COLLOCATION_NO_TRACES;
+  return h.cfg.precision == ADV_PRECISION_FP64 && h.cfg.diffusion == 0.0 &&
+         h.cfg.fused_form != ADV_FORM_COLLOCATION_NO_TRACES;
 }
 
 int ensure_traces(adv_handle *h)
 {
-  const size_t word = h->cfg.precision == ADV_PRECISION_FP64 ? sizeof(double) : sizeof(float);
-  const size_t nb   = (size_t)h->mesh.n_cells * 6 * h->mesh.n * h->mesh.n * word;
+  const size_t nb = (size_t)h->mesh.n_cells * 6 * h->mesh.n * h->mesh.n * sizeof(double);
   for (int i = 0; i < 2; ++i)
     if (!h->d_traces[i])
       {
@@ -769,7 +772,7 @@ int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, 
   if (gauss)
     {
       ADV_CUDA(adv::launch_basis_change(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, true, s,
-                                        traces ? tr_in : nullptr, h->cfg.precision != ADV_PRECISION_FP64));
+                                        traces ? static_cast<double *>(tr_in) : nullptr));
       ++h->launches;
     }
   for (int step = 0; step < n_steps; ++step)

@@ -81,10 +81,9 @@ cudaError_t upload_tables_gauss32(const DevTables<double> *d, const DevTables<fl
 // In-place change of basis of the cells [cell_begin, cell_end) of u:
 // to_gauss: Gauss-Lobatto nodal values -> values at the Gauss points (S x S x S);
 // otherwise the inverse (S^-1 x S^-1 x S^-1).  With traces (to_gauss only),
-// also writes the face traces of the result in the layout of StageArgs::tr_in
-// (binary32 with float_traces, for the FP32 operator).
+// also writes the face traces of the result in the layout of StageArgs::tr_in.
 cudaError_t launch_basis_change(int n, double *u, long long cell_begin, long long cell_end, bool to_gauss,
-                                cudaStream_t stream, void *traces = nullptr, bool float_traces = false);
+                                cudaStream_t stream, double *traces = nullptr);
 // cells processed per CTA by the stage kernel (for launch accounting)
 int stage_cells_per_block(int n, int precision);
 

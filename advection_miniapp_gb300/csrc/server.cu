@@ -288,7 +288,7 @@ int admit(adv_server *S, int64_t id)
       const size_t    tb    = (size_t)cells * 6 * q.npts * q.npts * sizeof(double);
       ADV_CUDA(cudaMallocAsync((void **)&q.t0, tb, g->stream));
       ADV_CUDA(cudaMallocAsync((void **)&q.t1, tb, g->stream));
-      ADV_CUDA(adv::launch_basis_change(q.npts, q.u, 0, cells, true, g->stream, q.t0, false));
+      ADV_CUDA(adv::launch_basis_change(q.npts, q.u, 0, cells, true, g->stream, q.t0));
       ++S->launches;
     }
   q.state   = 1;

@@ -20,11 +20,10 @@
 // The fused LSRK loop changes the basis of the solution once on entry and
 // once on exit (launch_basis_change); the stages in between run here.
 //
-// Face traces (TR, advection): a stage also writes the values at the face
-// points of its output that the next stage reads (r_out, or u_out on a last
-// stage), [6][n^2] per cell in the operator's precision; the next stage then
-// reads its own and its neighbours' face values instead of contracting
-// pencils.  Per cell-stage at
+// Face traces (TR, FP64 advection): a stage also writes the values at the
+// face points of its output that the next stage reads (r_out, or u_out on a
+// last stage), [6][n^2] per cell; the next stage then reads its own and its
+// neighbours' face values instead of contracting pencils.  Per cell-stage at
 // degree 4 the producer adds 750 FMAs and the consumer saves 1500; the
 // traces are the same contractions in the same order, so results are
 // bit-identical to the variant without them.
@@ -319,9 +318,11 @@ cudaError_t launch_stage_gauss_n(const StageArgs &args, cudaStream_t stream)
 {
   if (args.visc)
     return launch_stage_gauss_t<N, T, false, true, false>(args, stream);
-  if (args.tr_in)
-    return args.uniform ? launch_stage_gauss_t<N, T, true, false, true>(args, stream)
-                        : launch_stage_gauss_t<N, T, false, false, true>(args, stream);
+  // face traces: FP64 only (the library's choice; the kernel code is generic)
+  if constexpr (sizeof(T) == sizeof(double))
+    if (args.tr_in)
+      return args.uniform ? launch_stage_gauss_t<N, T, true, false, true>(args, stream)
+                          : launch_stage_gauss_t<N, T, false, false, true>(args, stream);
   return args.uniform ? launch_stage_gauss_t<N, T, true, false, false>(args, stream)
                       : launch_stage_gauss_t<N, T, false, false, false>(args, stream);
 }

@@ -8,9 +8,9 @@ namespace
 {
 // u <- (M x M x M) u per cell, M = S (to the Gauss points) or S^-1, through
 // shared memory: one thread per pencil, C cells per CTA
-template <int N, bool TO_GAUSS, typename TT = double>
+template <int N, bool TO_GAUSS>
 __global__ void __launch_bounds__(StageShape<N, double, true, false>::THREADS)
-  basis_kernel(double *u, long long cell_begin, long long cell_end, TT *traces)
+  basis_kernel(double *u, long long cell_begin, long long cell_end, double *traces)
 {
   using SH         = StageShape<N, double, true, false>;
   constexpr int C  = SH::C;
@@ -53,43 +53,37 @@ __global__ void __launch_bounds__(StageShape<N, double, true, false>::THREADS)
     g[i] = buf[i];
   if (TO_GAUSS && traces)
     {
-      // face traces of the result, [6][NF] per cell (StageArgs::tr_in), in
-      // the operator's precision TT: the values the first stage would load,
-      // contracted in that precision
+      // face traces of the result, [6][NF] per cell (StageArgs::tr_in)
       for (int w = tid; w < 3 * ncell * NF; w += NT)
         {
           const int d = w / (ncell * NF), v = w % (ncell * NF);
           const int cl = v / NF, r = v % NF;
           const int off = d == 0 ? N * r : d == 1 ? (r % N) + NF * (r / N) : r;
           const int st  = d == 0 ? 1 : d == 1 ? N : NF;
-          TT        x[N], lo, hi;
+          double    x[N], lo, hi;
 #pragma unroll
           for (int k = 0; k < N; ++k)
-            x[k] = from_double<TT>(buf[cl * NQ + off + k * st]);
-          pencil_traces<N, TT>(tab<TT>(N), x, lo, hi);
-          TT *to = traces + ((cell0 + cl) * 6 + 2 * d) * NF + r;
-          to[0]  = lo;
-          to[NF] = hi;
+            x[k] = buf[cl * NQ + off + k * st];
+          pencil_traces<N, double>(tb, x, lo, hi);
+          double *to = traces + ((cell0 + cl) * 6 + 2 * d) * NF + r;
+          to[0]      = lo;
+          to[NF]     = hi;
         }
     }
 }
 
 template <int N>
 cudaError_t launch_basis_n(double *u, long long cell_begin, long long cell_end, bool to_gauss, cudaStream_t s,
-                           void *traces, bool float_traces)
+                           double *traces)
 {
   using SH               = StageShape<N, double, true, false>;
   const long long blocks = (cell_end - cell_begin + SH::C - 1) / SH::C;
   if (blocks <= 0)
     return cudaSuccess;
-  if (!to_gauss)
-    basis_kernel<N, false, double><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, nullptr);
-  else if (float_traces)
-    basis_kernel<N, true, float>
-      <<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, static_cast<float *>(traces));
+  if (to_gauss)
+    basis_kernel<N, true><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, traces);
   else
-    basis_kernel<N, true, double>
-      <<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, static_cast<double *>(traces));
+    basis_kernel<N, false><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, nullptr);
   return cudaGetLastError();
 }
 } // namespace
@@ -105,16 +99,16 @@ cudaError_t launch_stage_gauss_fp64(int n, const StageArgs &args, cudaStream_t s
 }
 
 cudaError_t launch_basis_change(int n, double *u, long long cell_begin, long long cell_end, bool to_gauss,
-                                cudaStream_t stream, void *traces, bool float_traces)
+                                cudaStream_t stream, double *traces)
 {
   switch (n)
     {
-      case 2: return launch_basis_n<2>(u, cell_begin, cell_end, to_gauss, stream, traces, float_traces);
-      case 3: return launch_basis_n<3>(u, cell_begin, cell_end, to_gauss, stream, traces, float_traces);
-      case 4: return launch_basis_n<4>(u, cell_begin, cell_end, to_gauss, stream, traces, float_traces);
-      case 5: return launch_basis_n<5>(u, cell_begin, cell_end, to_gauss, stream, traces, float_traces);
-      case 6: return launch_basis_n<6>(u, cell_begin, cell_end, to_gauss, stream, traces, float_traces);
-      case 7: return launch_basis_n<7>(u, cell_begin, cell_end, to_gauss, stream, traces, float_traces);
+      case 2: return launch_basis_n<2>(u, cell_begin, cell_end, to_gauss, stream, traces);
+      case 3: return launch_basis_n<3>(u, cell_begin, cell_end, to_gauss, stream, traces);
+      case 4: return launch_basis_n<4>(u, cell_begin, cell_end, to_gauss, stream, traces);
+      case 5: return launch_basis_n<5>(u, cell_begin, cell_end, to_gauss, stream, traces);
+      case 6: return launch_basis_n<6>(u, cell_begin, cell_end, to_gauss, stream, traces);
+      case 7: return launch_basis_n<7>(u, cell_begin, cell_end, to_gauss, stream, traces);
       default: return cudaErrorInvalidValue;
     }
 }

@@ -17,7 +17,7 @@ import time
 
 import torch
 
-from . import (FORM_AUTO, FORM_COLLOCATION, FORM_NODAL, AdvectionOperation, IC_BLOB, IC_SINE_GAUSS, IC_WAVE, LSRK_3_3, LSRK_5_4, LSRK_7_4, LSRK_9_5,
+from . import (FORM_AUTO, FORM_COLLOCATION, FORM_COLLOCATION_NO_TRACES, FORM_NODAL, AdvectionOperation, IC_BLOB, IC_SINE_GAUSS, IC_WAVE, LSRK_3_3, LSRK_5_4, LSRK_7_4, LSRK_9_5,
                LowStorageRungeKuttaIntegrator, MESH_CARTESIAN, MESH_DEFORMED, PRECISION_FP32_OPERATOR,
                PRECISION_FP64, make_config, workload_config)
 
@@ -41,7 +41,7 @@ def parse(argv=None):
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--scheme", choices=sorted(SCHEMES), default="5_4")
     p.add_argument("--precision", choices=["fp64", "fp32"], default="fp64")
-    p.add_argument("--form", choices=["auto", "nodal", "collocation"], default="auto",
+    p.add_argument("--form", choices=["auto", "nodal", "collocation", "collocation-no-traces"], default="auto",
                    help="basis of the stages inside the fused step loop (fused_form)")
     p.add_argument("--flux-alpha", type=float, default=1.0)
     p.add_argument("--skew", type=float, default=0.0)
@@ -107,7 +107,8 @@ def main(argv=None):
                           deformation=args.deformation if args.mesh == "deformed" else 0.0,
                           velocity=tuple(args.velocity), initial_condition=ICS[args.initial_condition],
                           flux_alpha=args.flux_alpha, factor_skew=args.skew, precision=precision)
-    cfg.fused_form = {"auto": FORM_AUTO, "nodal": FORM_NODAL, "collocation": FORM_COLLOCATION}[args.form]
+    cfg.fused_form = {"auto": FORM_AUTO, "nodal": FORM_NODAL, "collocation": FORM_COLLOCATION,
+                      "collocation-no-traces": FORM_COLLOCATION_NO_TRACES}[args.form]
     op = AdvectionOperation(cfg)
     if args.implicit:
         res = run_implicit(args, op)
