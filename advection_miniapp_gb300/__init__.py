@@ -82,6 +82,13 @@ def lsrk_coefficients(scheme):
     return np.array(a[: n.value - 1]), np.array(b[: n.value])
 
 
+def write_vtu_host(config, values, time, path):
+    """VTU output of host values (numpy, n_dofs of the whole mesh); no GPU needed."""
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    _lib.check(_lib.load().adv_write_vtu_host(ctypes.byref(config), v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                              float(time), str(path).encode()), "adv_write_vtu_host")
+
+
 def _stream_handle(stream):
     import torch
     if stream is None:
@@ -206,6 +213,23 @@ class AdvectionOperation:
     def apply_mass(self, src, dst, stream=None):
         _lib.check(self._lib.adv_apply_mass(self._h, self._ptr(src), self._ptr(dst), _stream_handle(stream)),
                    "adv_apply_mass")
+
+    # -- output (advection_solver.cc:1220-1241) -----------------------------
+    def write_vtu(self, vec, time, path, stream=None):
+        """VTU file with "solution" and "analytic_solution" at the support points."""
+        _lib.check(self._lib.adv_write_vtu(self._h, self._ptr(vec), float(time), str(path).encode(),
+                                           _stream_handle(stream)), "adv_write_vtu")
+
+    def save_state(self, vec, time, path, stream=None):
+        _lib.check(self._lib.adv_save_state(self._h, self._ptr(vec), float(time), str(path).encode(),
+                                            _stream_handle(stream)), "adv_save_state")
+
+    def load_state(self, vec, path, stream=None):
+        """Fills vec from a state file of the same configuration; returns its time."""
+        t = ctypes.c_double()
+        _lib.check(self._lib.adv_load_state(self._h, self._ptr(vec), ctypes.byref(t), str(path).encode(),
+                                            _stream_handle(stream)), "adv_load_state")
+        return t.value
 
     # -- fused time stepping -------------------------------------------------
     def lsrk_steps(self, scheme, time, time_step, n_steps, solution, vec_ri, vec_ki, stream=None):

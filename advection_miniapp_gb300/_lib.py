@@ -87,6 +87,10 @@ SIGNATURES = {
     "adv_bdf2_step": (_I, [_P, _D, _D, _I, _P, _P, _P, _D, ctypes.POINTER(_I), _P]),
     "adv_create_slab": (_I, [ctypes.POINTER(AdvConfig), _I, _I, ctypes.POINTER(_P)]),
     "adv_slab_layout": (_I, [ctypes.POINTER(AdvConfig), _I, _I, ctypes.POINTER(_I64)]),
+    "adv_write_vtu": (_I, [_P, _P, _D, ctypes.c_char_p, _P]),
+    "adv_write_vtu_host": (_I, [ctypes.POINTER(AdvConfig), _DP, _D, ctypes.c_char_p]),
+    "adv_save_state": (_I, [_P, _P, _D, ctypes.c_char_p, _P]),
+    "adv_load_state": (_I, [_P, _P, _DP, ctypes.c_char_p, _P]),
     "adv_server_create": (_I, [_I64, _I, _I, _I, ctypes.POINTER(_P)]),
     "adv_server_destroy": (_I, [_P]),
     "adv_server_submit": (_I, [_P, ctypes.POINTER(AdvConfig), _D, _D, ctypes.POINTER(_I64)]),

@@ -17,7 +17,7 @@ LIB_PATH = os.path.join(HERE, "libadvection_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["tables.cpp", "geometry.cpp", "fdm.cpp", "api.cu", "implicit_api.cu", "stage_fp64.cu", "stage_fp32.cu",
-           "diag_kernels.cu", "implicit_kernels.cu", "batch_kernels.cu", "server.cu", "stage_gauss64.cu", "stage_gauss32.cu"]
+           "diag_kernels.cu", "implicit_kernels.cu", "batch_kernels.cu", "server.cu", "stage_gauss64.cu", "stage_gauss32.cu", "output.cu"]
 HEADERS = ["tables.h", "geometry.h", "fdm.h", "handle.h", "implicit_kernels.h", "batch_kernels.h", "kernels.h", "device_common.cuh", "stage_kernel.cuh", "stage_gauss.cuh"]
 
 

@@ -141,7 +141,7 @@ struct ExactParams
 // The initial condition translated with the constant velocity (for the
 // rotating field: the initial condition).  Mirrors ExactSolution::value
 // (advection_solver.cc:149-172) for the workloads' initial data.
-__device__ __forceinline__ double exact_value(const ExactParams &e, double x0, double x1, double x2,
+__host__ __device__ __forceinline__ double exact_value(const ExactParams &e, double x0, double x1, double x2,
                                               double t)
 {
   const double kPi = 3.14159265358979323846;

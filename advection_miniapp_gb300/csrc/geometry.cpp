@@ -143,6 +143,11 @@ void velocity_field(const adv_config &cfg, const double x[3], double b[3])
   b[2] = cfg.velocity[2];
 }
 
+void support_points(const adv_config &cfg, const Mesh &m, const Tables1D &tb, int64_t c, double *X)
+{
+  cell_support_points(cfg, m, tb, c, X);
+}
+
 int setup_mesh(const adv_config &cfg, Mesh &m)
 {
   m.n        = cfg.degree + 1;

@@ -73,6 +73,10 @@ void deform_point(const adv_config &cfg, const double L[3], const double x[3], d
 // Velocity field at x (spatial part; the rotating field's cos(pi t/T) factor is applied at run time).
 void velocity_field(const adv_config &cfg, const double x[3], double b[3]);
 
+// support points of local cell c (Gauss-Lobatto nodes through the mapping),
+// X[3 * (i + n (j + n k))]
+void support_points(const adv_config &cfg, const Mesh &m, const Tables1D &tb, int64_t c, double *X);
+
 int  setup_mesh(const adv_config &cfg, Mesh &m);
 // local mesh of the slab of global z layers [z_begin, z_end) with its ghost layers
 int  setup_slab(const adv_config &cfg, int z_begin, int z_end, Mesh &m);

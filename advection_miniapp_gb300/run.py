@@ -47,6 +47,9 @@ def parse(argv=None):
     p.add_argument("--skew", type=float, default=0.0)
     p.add_argument("--output-every", type=int, default=0, help="0: only at the start and the end")
     p.add_argument("--json", action="store_true", help="print one JSON summary line")
+    p.add_argument("--vtu", default=None, metavar="PREFIX",
+                   help="write PREFIX_NNN.vtu (solution and analytic solution) at every output step")
+    p.add_argument("--save-state", default=None, metavar="PATH", help="write the final state for a restart")
     p.add_argument("--compare-fp64", action="store_true",
                    help="FP32 operator: rerun with the FP64 operator and report both errors and the difference")
     p.add_argument("--implicit", action="store_true",
@@ -133,9 +136,14 @@ def main(argv=None):
     op.project_initial(u)
     r, k = op.initialize_dof_vector(), op.initialize_dof_vector()
 
+    n_out = [0]
+
     def output(step, t):
         err, nrm = op.l2_error(u, t)
         me = op.compute_mass_and_energy(u)
+        if args.vtu:
+            op.write_vtu(u, t, f"{args.vtu}_{n_out[0]:03d}.vtu")
+            n_out[0] += 1
         if not args.json:
             print(f"   Time {t:8.3g}  error {err / nrm:10.5g}  mass {me[0]:16.10g}  energy {me[1]:16.10g}"
                   f"  H1-semi {me[2]:9.4g}")
@@ -160,6 +168,8 @@ def main(argv=None):
         t = step * dt
         if args.output_every > 0 or step == args.steps:
             rel, me = output(step, t)
+    if args.save_state:
+        op.save_state(u, t, args.save_state)
     per_step = wall / max(args.steps, 1)
     stage_rate = op.n_dofs * integ.n_stages() * args.steps / wall / 1e9 if wall > 0 else 0.0
     res = {"workload": args.workload, "precision": args.precision, "n_dofs": op.n_dofs, "steps": args.steps,

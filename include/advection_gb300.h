@@ -214,6 +214,18 @@ int adv_fgmres(adv_solver *s, double mass_factor, double t, const double *rhs, d
 int adv_bdf2_step(adv_solver *s, double t_new, double dt, int first_step, const double *u_n, const double *u_nm1,
                   double *u_new, double rel_tol, int *iterations, void *stream);
 
+/* ------------------------------------------------------------------ output
+ * output_results (advection_solver.cc:1220-1241): a VTU file with the
+ * support points of every (owned) cell, k^3 hexahedra per cell and the point
+ * fields "solution" and "analytic_solution" (exact solution at time t). */
+int adv_write_vtu(adv_handle *h, const double *vec, double time, const char *path, void *stream);
+/* The same from host values of the whole mesh (no device needed). */
+int adv_write_vtu_host(const adv_config *cfg, const double *host_vec, double time, const char *path);
+/* Raw state for restart: header (degree, cells, mesh type, time) + the owned
+ * nodal values; adv_load_state rejects files of another configuration. */
+int adv_save_state(adv_handle *h, const double *vec, double time, const char *path, void *stream);
+int adv_load_state(adv_handle *h, double *vec, double *time, const char *path, void *stream);
+
 /* ------------------------------------------------------------- serving loop
  * Continuous batching of independent solves on one GPU (no counterpart in the
  * reference, which runs one solve per program).  Requests (periodic affine n^3
