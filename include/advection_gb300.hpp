@@ -149,6 +149,22 @@ public:
     return dt;
   }
 
+  // output_results (advection_solver.cc:1220-1241)
+  void write_vtu(const DeviceVector &vec, const double t, const std::string &path) const
+  {
+    check(adv_write_vtu(h_, vec.data(), t, path.c_str(), stream_), "write_vtu");
+  }
+  void save_state(const DeviceVector &vec, const double t, const std::string &path) const
+  {
+    check(adv_save_state(h_, vec.data(), t, path.c_str(), stream_), "save_state");
+  }
+  double load_state(DeviceVector &vec, const std::string &path) const
+  {
+    double t = 0;
+    check(adv_load_state(h_, vec.data(), &t, path.c_str(), stream_), "load_state");
+    return t;
+  }
+
   adv_handle  *handle() const { return h_; }
   cudaStream_t stream() const { return stream_; }
 
