@@ -42,7 +42,14 @@ struct GaussShape
   // the nodal layout plus, with traces, Tb [C][6][NF] own face values,
   // padded to 16 bytes: the geometry after it is filled by 16-byte cp.async
   static constexpr int TB_VALUES = TR ? (6 * C * N * N * (int)sizeof(T) + 15) / 16 * 16 / (int)sizeof(T) : 0;
-  static constexpr int SMEM      = SH::SMEM + TB_VALUES * (int)sizeof(T);
+  // field geometry with traces: the face coefficients are read from global
+  // memory in the direction passes (one read per face point) instead of being
+  // staged, which frees 12 C n^2 values of shared memory per CTA (one more
+  // resident CTA per SM at degree 4)
+  static constexpr bool FACES_GLOBAL = TR && !UNI && !VISC;
+  static constexpr int  FB_VALUES    = UNI || FACES_GLOBAL ? 0 : 12 * C * N * N;
+  static constexpr int  SMEM = SH::SMEM + TB_VALUES * (int)sizeof(T) -
+                              (UNI ? 0 : (12 * C * N * N - FB_VALUES) * (int)sizeof(T));
   // byte offset of the cell geometry Gb in the layout of stage_gauss_cta
   static constexpr int GB_OFFSET = (2 * C * N * N * N + 6 * C * N * N + TB_VALUES) * (int)sizeof(T);
   static_assert(GB_OFFSET % 16 == 0, "cp.async destinations need 16-byte alignment");
@@ -63,8 +70,10 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
   T   *Nb     = Qb + C * NQ;                     // [C][6][NF] neighbour values at the face points
   T   *Tb     = Nb + C * 6 * NF;                 // traces: [C][6][NF] own values at the face points
   T   *Gb     = Tb + GaussShape<N, T, UNI, VISC, TR>::TB_VALUES; // field: [C][4][NQ] cell geometry
-  T   *Fb     = Gb + (UNI ? 0 : C * 4 * NQ);     // field: [C][6][2][NF] face coefficients
-  T   *Nd     = Fb + (UNI ? 0 : C * 12 * NF);    // viscous: [C][6][NF] neighbour normal derivatives
+  using GS                 = GaussShape<N, T, UNI, VISC, TR>;
+  constexpr bool FG        = GS::FACES_GLOBAL;
+  T   *Fb     = Gb + (UNI ? 0 : C * 4 * NQ);     // field: [C][6][2][NF] face coefficients (staged unless FG)
+  T   *Nd     = Fb + GS::FB_VALUES;              // viscous: [C][6][NF] neighbour normal derivatives
   int *s_nbr  = reinterpret_cast<int *>(Nd + (VISC ? C * 6 * NF : 0));
   int *s_face = s_nbr + C * 6;
 
@@ -75,7 +84,18 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
   cell_neighbours(A, cell0, ncell, s_nbr, s_face, tid, NT);
   __syncthreads();
   if (!UNI)
-    geometry_async<N, T>(A, cell0, ncell, s_face, Gb, Fb, tid, NT);
+    geometry_async<N, T>(A, cell0, ncell, s_face, Gb, Fb, tid, NT, !FG);
+
+  // face coefficients [P | M] of face j of local cell cl: staged or global
+  auto faces = [&](int cl, int j) -> const T * {
+    if (FG)
+      {
+        const int d = j >> 1;
+        const T  *F = static_cast<const T *>(d == 0 ? A.face_geo[0] : d == 1 ? A.face_geo[1] : A.face_geo[2]);
+        return F + (size_t)s_face[cl * 6 + j] * 2 * NF;
+      }
+    return Fb + (cl * 6 + j) * 2 * NF;
+  };
 
   // ---- phase 1: own values (one contiguous range of the CTA's cells) and
   //      the neighbours' values at the face points
@@ -153,12 +173,12 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
 #pragma unroll
       for (int k = 0; k < N; ++k)
         U[k] = p[k];
-      const T *F  = Fb + cl * 12 * NF;
       const T *Tr = Tb + cl * 6 * NF + r;
       direction_pass<N, T, UNI, VISC, 0, TR>(A, tb, U, Nb[(cl * 6 + 0) * NF + r], Nb[(cl * 6 + 1) * NF + r],
                                              VISC ? Nd[(cl * 6 + 0) * NF + r] : T(0),
                                              VISC ? Nd[(cl * 6 + 1) * NF + r] : T(0), s_nbr[cl * 6 + 0] < 0,
-                                             s_nbr[cl * 6 + 1] < 0, r, F, F + 2 * NF, Gb + cl * 4 * NQ + N * r,
+                                             s_nbr[cl * 6 + 1] < 0, r, faces(cl, 0), faces(cl, 1),
+                                             Gb + cl * 4 * NQ + N * r,
                                              1, out, TR ? Tr[0] : T(0), TR ? Tr[NF] : T(0));
       T *z = Qb + cl * NQ + N * r;
 #pragma unroll
@@ -177,12 +197,11 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
 #pragma unroll
       for (int k = 0; k < N; ++k)
         U[k] = p[k * N];
-      const T *F  = Fb + cl * 12 * NF + 4 * NF;
       const T *Tr = Tb + cl * 6 * NF + 2 * NF + r;
       direction_pass<N, T, UNI, VISC, 1, TR>(A, tb, U, Nb[(cl * 6 + 2) * NF + r], Nb[(cl * 6 + 3) * NF + r],
                                              VISC ? Nd[(cl * 6 + 2) * NF + r] : T(0),
                                              VISC ? Nd[(cl * 6 + 3) * NF + r] : T(0), s_nbr[cl * 6 + 2] < 0,
-                                             s_nbr[cl * 6 + 3] < 0, r, F, F + 2 * NF,
+                                             s_nbr[cl * 6 + 3] < 0, r, faces(cl, 2), faces(cl, 3),
                                              Gb + (cl * 4 + 1) * NQ + off, N, out, TR ? Tr[0] : T(0),
                                              TR ? Tr[NF] : T(0));
       T *z = Qb + cl * NQ + off;
@@ -202,13 +221,13 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
 #pragma unroll
       for (int k = 0; k < N; ++k)
         U[k] = p[k * NF];
-      const T *F  = Fb + cl * 12 * NF + 8 * NF;
       const T *G  = Gb + cl * 4 * NQ;
       const T *Tr = Tb + cl * 6 * NF + 4 * NF + r;
       direction_pass<N, T, UNI, VISC, 2, TR>(A, tb, U, Nb[(cl * 6 + 4) * NF + r], Nb[(cl * 6 + 5) * NF + r],
                                              VISC ? Nd[(cl * 6 + 4) * NF + r] : T(0),
                                              VISC ? Nd[(cl * 6 + 5) * NF + r] : T(0), s_nbr[cl * 6 + 4] < 0,
-                                             s_nbr[cl * 6 + 5] < 0, r, F, F + 2 * NF, G + 2 * NQ + r, NF, out,
+                                             s_nbr[cl * 6 + 5] < 0, r, faces(cl, 4), faces(cl, 5), G + 2 * NQ + r,
+                                             NF, out,
                                              TR ? Tr[0] : T(0), TR ? Tr[NF] : T(0));
       T              *z  = Qb + cl * NQ + r;
       const long long gb = (cell0 + cl) * NQ + r;

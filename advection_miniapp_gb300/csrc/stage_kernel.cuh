@@ -404,7 +404,7 @@ __device__ __forceinline__ void cell_neighbours(const StageArgs &A, long long ce
 // group; the caller waits with __pipeline_wait_prior(0) before using them.
 template <int N, typename T>
 __device__ __forceinline__ void geometry_async(const StageArgs &A, long long cell0, int ncell, const int *s_face,
-                                               T *Gb, T *Fb, int tid, int nthreads)
+                                               T *Gb, T *Fb, int tid, int nthreads, bool faces = true)
 {
   constexpr int NQ  = N * N * N;
   constexpr int NF  = N * N;
@@ -413,7 +413,7 @@ __device__ __forceinline__ void geometry_async(const StageArgs &A, long long cel
   for (int i = tid; i < n16; i += nthreads)
     __pipeline_memcpy_async(reinterpret_cast<char *>(Gb) + 16 * i, geo + 16 * i, 16);
   constexpr int F8 = 2 * NF * (int)sizeof(T) / 8; // 8-byte chunks per cell-face
-  for (int i = tid; i < ncell * 6 * F8; i += nthreads)
+  for (int i = tid; faces && i < ncell * 6 * F8; i += nthreads)
     {
       const int cf = i / F8, e = i % F8;
       const int d  = (cf % 6) >> 1;
