@@ -15,7 +15,8 @@ from ._lib import (AdvConfig, AdvError, BOUNDARY_EXACT, BOUNDARY_ZERO, FORM_AUTO
                    FORM_NODAL,
                    IC_BLOB, IC_SINE_GAUSS,
                    IC_WAVE, LSRK_3_3, LSRK_5_4, LSRK_7_4, LSRK_9_5, MESH_CARTESIAN, MESH_DEFORMED,
-                   PRECISION_FP32_OPERATOR, PRECISION_FP64, VELOCITY_CONSTANT, VELOCITY_ROTATING)
+                   PRECISION_FP32_INCREMENT, PRECISION_FP32_OPERATOR, PRECISION_FP64, VELOCITY_CONSTANT,
+                   VELOCITY_ROTATING)
 
 __all__ = [
     "AdvConfig", "AdvError", "AdvectionOperation", "ImplicitSolver", "LowStorageRungeKuttaIntegrator", "make_config",

@@ -17,7 +17,7 @@ MESH_CARTESIAN, MESH_DEFORMED = 0, 1
 VELOCITY_CONSTANT, VELOCITY_ROTATING = 0, 1
 IC_SINE_GAUSS, IC_BLOB, IC_WAVE = 0, 1, 2
 BOUNDARY_ZERO, BOUNDARY_EXACT = 0, 1
-PRECISION_FP64, PRECISION_FP32_OPERATOR = 0, 1
+PRECISION_FP64, PRECISION_FP32_OPERATOR, PRECISION_FP32_INCREMENT = 0, 1, 2
 LSRK_3_3, LSRK_5_4, LSRK_7_4, LSRK_9_5 = 0, 1, 2, 3
 FORM_AUTO, FORM_NODAL, FORM_COLLOCATION, FORM_COLLOCATION_NO_TRACES = 0, 1, 2, 3
 

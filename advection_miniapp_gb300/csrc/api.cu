@@ -194,7 +194,8 @@ int validate(const adv_config &c)
     return fail(ADV_ERR_INVALID, "unknown initial_condition");
   if (c.initial_condition == ADV_IC_BLOB && !(c.ic_params[3] > 0.0))
     return fail(ADV_ERR_INVALID, "blob width ic_params[3] must be positive");
-  if (c.precision != ADV_PRECISION_FP64 && c.precision != ADV_PRECISION_FP32_OPERATOR)
+  if (c.precision != ADV_PRECISION_FP64 && c.precision != ADV_PRECISION_FP32_OPERATOR &&
+      c.precision != ADV_PRECISION_FP32_INCREMENT)
     return fail(ADV_ERR_INVALID, "unknown precision");
   if (c.diffusion < 0.0)
     return fail(ADV_ERR_INVALID, "diffusion must be >= 0");
@@ -286,11 +287,19 @@ double time_factor(const adv_handle &h, double t)
   return std::cos(3.14159265358979323846 * t / h.cfg.velocity_period);
 }
 
-adv::StageArgs base_args(const adv_handle &h, double t)
+// precision of the operator kernels of a handle: FP64 (0) or FP32 (1)
+int op_precision(const adv_handle &h)
+{
+  return h.cfg.precision == ADV_PRECISION_FP64 ? 0 : 1;
+}
+
+adv::StageArgs base_args(const adv_handle &h, double t, int prec = -1)
 {
   adv::StageArgs A;
   std::memset(&A, 0, sizeof(A));
   const adv::Mesh &m = h.mesh;
+  // the FP64 anchor stage of an FP32-increment handle uses the FP64 copy
+  const bool geo64 = prec == 0 && op_precision(h) == 1;
   for (int d = 0; d < 3; ++d)
     {
       A.nc[d]   = m.nc[d];
@@ -301,7 +310,7 @@ adv::StageArgs base_args(const adv_handle &h, double t)
       A.cvf[d]  = (float)h.cv[d];
       A.Pf[d]   = (float)h.P[d];
       A.Mf[d]   = (float)h.M[d];
-      A.face_geo[d] = h.d_face_geo[d];
+      A.face_geo[d] = geo64 ? (const void *)h.d_face_geo64[d] : h.d_face_geo[d];
       A.face_x[d]   = h.d_face_x[d];
     }
   A.n_cells    = m.cell_end;
@@ -312,7 +321,7 @@ adv::StageArgs base_args(const adv_handle &h, double t)
   A.skew     = h.cfg.factor_skew;
   A.skewf    = (float)h.cfg.factor_skew;
   A.has_skew = h.cfg.factor_skew != 0.0;
-  A.cell_geo = h.d_cell_geo;
+  A.cell_geo = geo64 ? (const void *)h.d_cell_geo64 : h.d_cell_geo;
   A.t        = t;
   A.ex       = h.diag.ex;
   const double s = time_factor(h, t);
@@ -341,9 +350,9 @@ adv::StageArgs base_args(const adv_handle &h, double t)
   return A;
 }
 
-int launch(adv_handle *h, const adv::StageArgs &A, cudaStream_t s)
+int launch(adv_handle *h, const adv::StageArgs &A, cudaStream_t s, int prec = -1)
 {
-  const bool  fp64 = h->cfg.precision == ADV_PRECISION_FP64;
+  const bool  fp64 = (prec < 0 ? op_precision(*h) : prec) == 0;
   cudaError_t e    = A.gauss ? (fp64 ? adv::launch_stage_gauss_fp64(h->mesh.n, A, s)
                                      : adv::launch_stage_gauss_fp32(h->mesh.n, A, s))
                              : (fp64 ? adv::launch_stage_fp64(h->mesh.n, A, s)
@@ -416,7 +425,7 @@ namespace adv
 {
 namespace detail
 {
-adv::StageArgs base_args(const adv_handle &h, double t) { return ::base_args(h, t); }
+adv::StageArgs base_args(const adv_handle &h, double t, int op_precision) { return ::base_args(h, t, op_precision); }
 int            launch(adv_handle *h, const adv::StageArgs &A, cudaStream_t s) { return ::launch(h, A, s); }
 int            check_device(const adv_handle *h) { return ::check_device(h); }
 int            ensure_tables(int device) { return ::ensure_tables(device); }
@@ -487,14 +496,23 @@ int create_handle(const adv_config *cfg, int z_begin, int z_end, adv_handle **ou
       for (int d = 0; d < 3; ++d)
         h->cv[d] = g.cv[d], h->P[d] = g.P[d], h->M[d] = g.M[d];
       const bool fp64 = h->cfg.precision == ADV_PRECISION_FP64;
+      const bool both = h->cfg.precision == ADV_PRECISION_FP32_INCREMENT;
       if (!g.cell.empty())
-        rc = fp64 ? upload_array<double>(g.cell, &h->d_cell_geo, h->device_bytes)
-                  : upload_array<float>(g.cell, &h->d_cell_geo, h->device_bytes);
+        {
+          rc = fp64 ? upload_array<double>(g.cell, &h->d_cell_geo, h->device_bytes)
+                    : upload_array<float>(g.cell, &h->d_cell_geo, h->device_bytes);
+          if (rc == ADV_OK && both)
+            rc = upload_array<double>(g.cell, (void **)&h->d_cell_geo64, h->device_bytes);
+        }
       for (int d = 0; d < 3 && rc == ADV_OK; ++d)
         {
           if (!g.face[d].empty())
-            rc = fp64 ? upload_array<double>(g.face[d], &h->d_face_geo[d], h->device_bytes)
-                      : upload_array<float>(g.face[d], &h->d_face_geo[d], h->device_bytes);
+            {
+              rc = fp64 ? upload_array<double>(g.face[d], &h->d_face_geo[d], h->device_bytes)
+                        : upload_array<float>(g.face[d], &h->d_face_geo[d], h->device_bytes);
+              if (rc == ADV_OK && both)
+                rc = upload_array<double>(g.face[d], (void **)&h->d_face_geo64[d], h->device_bytes);
+            }
           if (rc == ADV_OK && !g.face_x[d].empty())
             rc = upload_array<double>(g.face_x[d], (void **)&h->d_face_x[d], h->device_bytes);
         }
@@ -572,6 +590,9 @@ int adv_destroy(adv_handle *h)
   if (!h)
     return ADV_OK;
   cudaFree(h->d_cell_geo);
+  cudaFree(h->d_cell_geo64);
+  for (int d = 0; d < 3; ++d)
+    cudaFree(h->d_face_geo64[d]);
   for (int d = 0; d < 3; ++d)
     {
       cudaFree(h->d_face_geo[d]);
@@ -740,6 +761,83 @@ int adv_lsrk_coefficients(int scheme, double *a, double *b, int *n_stages)
 // written by the previous stage, write the next r to the other one and
 // update U in place.  No stage writes a buffer that neighbouring cells read,
 // and the solution ends in U without copies.
+namespace
+{
+// FP32 increments (ADV_PRECISION_FP32_INCREMENT): per step, stage 0 with the
+// FP64 operator writes K0 = L(u_n), E = b0 dt K0 and G = a0 dt K0 (the
+// increments u - u_n and r - u_n); stages s >= 1 evaluate k = K0 + L32(G_s)
+// and update E and G in FP64; the last stage writes u_n + E + b dt k into u.
+// Buffers: E = r, G alternates between k and a handle scratch vector, K0 in
+// a second scratch vector.
+int lsrk_increment_steps(adv_handle *h, const std::vector<double> &ai, const std::vector<double> &bi, double t,
+                         double dt, int n_steps, double *u, double *r, double *k, cudaStream_t s)
+{
+  if (int e = ensure_scratch(h, 0))
+    return e;
+  if (int e = ensure_scratch(h, 1))
+    return e;
+  const bool gauss = n_steps > 0 && h->cfg.fused_form != ADV_FORM_NODAL;
+  double    *E = r, *Ga = k, *Gb = h->d_scratch[0], *K0 = h->d_scratch[1];
+  const int  ns = (int)bi.size();
+  if (gauss)
+    {
+      ADV_CUDA(adv::launch_basis_change(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, true, s));
+      ++h->launches;
+    }
+  for (int step = 0; step < n_steps; ++step)
+    {
+      const double t0 = t + step * dt;
+      double       sum_previous_bi = 0.0;
+      for (int st = 0; st < ns; ++st)
+        {
+          double ts = t0;
+          if (st > 0)
+            {
+              ts = t0 + (sum_previous_bi + ai[st - 1]) * dt;
+              sum_previous_bi += bi[st - 1];
+            }
+          const int      prec = st == 0 ? 0 : 1;
+          adv::StageArgs A    = base_args(*h, ts, prec);
+          const bool     last = st == ns - 1;
+          A.gauss             = gauss;
+          A.b                 = bi[st] * dt * A.out_scale;
+          A.a                 = last ? 0.0 : ai[st] * dt * A.out_scale;
+          A.mode              = last ? adv::kModeLastStage : adv::kModeStage;
+          if (st == 0)
+            {
+              A.r_in = u, A.u_in = nullptr, A.u_out = E, A.r_out = Ga, A.k_out = K0;
+            }
+          else
+            {
+              A.r_in  = (st % 2) ? Ga : Gb;
+              A.k_add = K0;
+              A.u_in  = E;
+              if (last)
+                A.u_out = u, A.u_base = u;
+              else
+                A.u_out = E, A.r_out = (st % 2) ? Gb : Ga;
+            }
+          if (int e = launch(h, A, s, prec))
+            return e;
+        }
+    }
+  if (gauss)
+    {
+      ADV_CUDA(adv::launch_basis_change(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, false, s));
+      ++h->launches;
+    }
+  return ADV_OK;
+}
+
+// the increment form is exact for operators linear in u and independent of
+// time: constant velocity, no inhomogeneous (exact) Dirichlet data
+bool increment_form_applies(const adv_handle &h)
+{
+  return h.cfg.precision == ADV_PRECISION_FP32_INCREMENT && h.cfg.velocity_type == ADV_VELOCITY_CONSTANT &&
+         (h.mesh.periodic || h.cfg.boundary_value != ADV_BOUNDARY_EXACT);
+}
+} // namespace
+
 int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, double *u, double *r,
                    double *k, void *stream)
 {
@@ -761,6 +859,8 @@ int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, 
   const int    ns = (int)bi.size();
   if (ns == 1)
     return fail(ADV_ERR_INVALID, "one-stage schemes are not supported");
+  if (increment_form_applies(*h))
+    return lsrk_increment_steps(h, ai, bi, t, dt, n_steps, u, r, k, s);
   // collocation form: the solution moves to the Gauss-point values for the
   // steps and back afterwards (r and k are scratch either way)
   const bool gauss  = n_steps > 0 && use_collocation(*h);

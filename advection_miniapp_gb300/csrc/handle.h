@@ -21,8 +21,10 @@ struct adv_handle
   // uniform-case constants
   double cv[3] = {}, P[3] = {}, M[3] = {};
   // device buffers
-  void    *d_cell_geo    = nullptr;
+  void    *d_cell_geo    = nullptr;     // field geometry in the operator's precision
   void    *d_face_geo[3] = {};
+  double  *d_cell_geo64    = nullptr;   // FP32 increments: the FP64 copy for the anchor stage
+  double  *d_face_geo64[3] = {};
   double  *d_face_x[3]   = {};
   double  *d_partials    = nullptr;
   double  *d_scratch[2]  = {};
@@ -42,7 +44,9 @@ namespace detail
 {
 int            fail(int code, const std::string &msg);
 int            cuda_fail(cudaError_t e, const char *where);
-adv::StageArgs base_args(const adv_handle &h, double t);
+// stage arguments at time t for the operator precision op_precision
+// (0 = FP64, 1 = FP32; -1 = the handle's own)
+adv::StageArgs base_args(const adv_handle &h, double t, int op_precision = -1);
 int            launch(adv_handle *h, const adv::StageArgs &A, cudaStream_t s);
 int            check_device(const adv_handle *h);
 // uploads the 1D tables to every translation unit on this device (once)

@@ -63,6 +63,11 @@ struct StageArgs
   // the operator's precision
   const void   *tr_in;
   void         *tr_out;
+  // FP32 increments (optional): k += k_add before the update; k_out receives
+  // k; the last stage adds u_base to its output; u_in == nullptr reads as 0
+  const double *k_add;
+  double       *k_out;
+  const double *u_base;
   ExactParams   ex;
 };
 

@@ -238,21 +238,27 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
           T zz = z[k * NF] + out[k];
           if (!UNI)
             zz *= G[3 * NQ + r + k * NF];
-          const double    kd = to_double<T>(zz);
           const long long gi = gb + k * NF;
+          double          kd = to_double<T>(zz);
+          if (!TR && A.k_add)
+            kd += __ldcs(A.k_add + gi);
           if (A.mode == kModeStage)
             {
-              const double u = __ldcs(A.u_in + gi);
+              const double u  = (TR || A.u_in) ? __ldcs(A.u_in + gi) : 0.0;
               const double rn = fma(A.a, kd, u);
-              A.u_out[gi]    = fma(A.b, kd, u);
-              A.r_out[gi]    = rn;
-              next[k]        = rn;
+              A.u_out[gi]     = fma(A.b, kd, u);
+              A.r_out[gi]     = rn;
+              next[k]         = rn;
+              if (!TR && A.k_out)
+                A.k_out[gi] = kd;
             }
           else if (A.mode == kModeLastStage)
             {
-              const double un = fma(A.b, kd, __ldcs(A.u_in + gi));
-              A.u_out[gi]     = un;
-              next[k]         = un;
+              double un = fma(A.b, kd, __ldcs(A.u_in + gi));
+              if (!TR && A.u_base)
+                un += A.u_base[gi];
+              A.u_out[gi] = un;
+              next[k]     = un;
             }
           else
             {

@@ -746,16 +746,28 @@ __device__ __forceinline__ void stage_cta(const StageArgs &A, const long long ce
     {
       for (int i = tid; i < ncell * NQ; i += NT)
         {
-          const double kd = to_double<T>(Qb[i]);
-          const double u  = __ldcs(A.u_in + g0 + i);
+          double kd = to_double<T>(Qb[i]);
+          if (A.k_add)
+            kd += __ldcs(A.k_add + g0 + i);
+          const double u  = A.u_in ? __ldcs(A.u_in + g0 + i) : 0.0;
           A.u_out[g0 + i] = fma(A.b, kd, u);
           A.r_out[g0 + i] = fma(A.a, kd, u);
+          if (A.k_out)
+            A.k_out[g0 + i] = kd;
         }
     }
   else
     {
       for (int i = tid; i < ncell * NQ; i += NT)
-        A.u_out[g0 + i] = fma(A.b, to_double<T>(Qb[i]), __ldcs(A.u_in + g0 + i));
+        {
+          double kd = to_double<T>(Qb[i]);
+          if (A.k_add)
+            kd += __ldcs(A.k_add + g0 + i);
+          double v = fma(A.b, kd, __ldcs(A.u_in + g0 + i));
+          if (A.u_base)
+            v += A.u_base[g0 + i];
+          A.u_out[g0 + i] = v;
+        }
     }
 }
 

@@ -268,6 +268,62 @@ def test_fp32_operator_l2_error_matches_fp64(cuda, adv_lib):
     assert errs[1] <= 1.05 * errs[0], errs
 
 
+@pytest.mark.parametrize("form", [1, 2])
+@pytest.mark.parametrize("case", ["curved-k4", "affine-k3", "affine-k6", "sipg-periodic-k2", "box-domain",
+                                  "affine-k2-central"])
+def test_fp32_increment_form_against_oracle(cuda, oracle_mod, adv_lib, case, form):
+    """FP32 increments (one FP64 operator per step, FP32 operators on r - u_n):
+    close to the FP64 oracle, far closer than the plain FP32 operator."""
+    torch = cuda
+    cfg = CASES[case]
+    o = oracle_mod.Oracle(**cfg)
+    dt = o.time_step(0.5)
+    u = o.project(0.0)
+    r, k = o.zeros(), o.zeros()
+    for s in range(4):
+        o.lsrk_step(s * dt, dt, u, r, k)
+    errs = {}
+    for precision in (adv_lib.PRECISION_FP32_OPERATOR, adv_lib.PRECISION_FP32_INCREMENT):
+        g = adv_lib.AdvectionOperation(**cfg, precision=precision, fused_form=form)
+        ud = g.initialize_dof_vector()
+        g.project_initial(ud)
+        rd, kd = g.initialize_dof_vector(), g.initialize_dof_vector()
+        g.lsrk_steps(adv_lib.LSRK_5_4, 0.0, dt, 4, ud, rd, kd)
+        errs[precision] = rel_err(ud.cpu().numpy(), u)
+    assert errs[adv_lib.PRECISION_FP32_INCREMENT] <= 2e-9, errs
+    assert errs[adv_lib.PRECISION_FP32_INCREMENT] <= 0.05 * errs[adv_lib.PRECISION_FP32_OPERATOR], errs
+
+
+def test_fp32_increment_form_falls_back_for_time_dependent_operators(cuda, oracle_mod, adv_lib):
+    """Rotating velocity (time-dependent operator): the plain FP32 operator runs."""
+    cfg = CASES["rotating-k3"]
+    res = []
+    for precision in (adv_lib.PRECISION_FP32_OPERATOR, adv_lib.PRECISION_FP32_INCREMENT):
+        g = adv_lib.AdvectionOperation(**cfg, precision=precision)
+        ud = g.initialize_dof_vector()
+        g.project_initial(ud)
+        rd, kd = g.initialize_dof_vector(), g.initialize_dof_vector()
+        g.lsrk_steps(adv_lib.LSRK_5_4, 0.0, g.time_step(0.5), 3, ud, rd, kd)
+        res.append(ud.cpu().numpy())
+    np.testing.assert_array_equal(res[0], res[1])
+
+
+def test_fp32_increment_l2_error_equals_fp64_at_fine_resolution(cuda, adv_lib):
+    """32^3 curved cells of degree 4, 40 steps: the plain FP32 operator's round-off
+    shows in the L2 error, the increment form matches FP64 within 1.05x."""
+    errs = {}
+    for precision in (0, 1, 2):
+        g = adv_lib.AdvectionOperation(adv_lib.workload_config("deformed-k4-32", precision=precision))
+        dt = g.time_step(0.5)
+        u = g.initialize_dof_vector()
+        g.project_initial(u)
+        r, k = g.initialize_dof_vector(), g.initialize_dof_vector()
+        g.lsrk_steps(adv_lib.LSRK_5_4, 0.0, dt, 40, u, r, k)
+        e, n = g.l2_error(u, 40 * dt)
+        errs[precision] = e / n
+    assert errs[2] <= 1.05 * errs[0], errs
+
+
 def test_full_size_curved_properties(cuda, adv_lib):
     """64^3 curved, degree 4 (32.8M DoFs): mass conserved, energy non-increasing,
     FP32-operator result close to FP64 after a few steps."""
