@@ -18,7 +18,8 @@ import time
 import torch
 
 from . import (FORM_AUTO, FORM_COLLOCATION, FORM_COLLOCATION_NO_TRACES, FORM_NODAL, AdvectionOperation, IC_BLOB, IC_SINE_GAUSS, IC_WAVE, LSRK_3_3, LSRK_5_4, LSRK_7_4, LSRK_9_5,
-               LowStorageRungeKuttaIntegrator, MESH_CARTESIAN, MESH_DEFORMED, PRECISION_FP32_OPERATOR,
+               LowStorageRungeKuttaIntegrator, MESH_CARTESIAN, MESH_DEFORMED, PRECISION_FP32_INCREMENT,
+               PRECISION_FP32_OPERATOR,
                PRECISION_FP64, make_config, workload_config)
 
 SCHEMES = {"3_3": LSRK_3_3, "5_4": LSRK_5_4, "7_4": LSRK_7_4, "9_5": LSRK_9_5}
@@ -40,7 +41,9 @@ def parse(argv=None):
     p.add_argument("--courant", type=float, default=0.5)
     p.add_argument("--steps", type=int, default=200)
     p.add_argument("--scheme", choices=sorted(SCHEMES), default="5_4")
-    p.add_argument("--precision", choices=["fp64", "fp32"], default="fp64")
+    p.add_argument("--precision", choices=["fp64", "fp32", "fp32-increment"], default="fp64",
+                   help="FP64 operator, FP32 operator, or FP32 operator on the stage increments with one FP64 "
+                        "evaluation per step")
     p.add_argument("--form", choices=["auto", "nodal", "collocation", "collocation-no-traces"], default="auto",
                    help="basis of the stages inside the fused step loop (fused_form)")
     p.add_argument("--flux-alpha", type=float, default=1.0)
@@ -101,7 +104,8 @@ def run_implicit(args, op):
 
 def main(argv=None):
     args = parse(argv)
-    precision = PRECISION_FP64 if args.precision == "fp64" else PRECISION_FP32_OPERATOR
+    precision = {"fp64": PRECISION_FP64, "fp32": PRECISION_FP32_OPERATOR,
+                 "fp32-increment": PRECISION_FP32_INCREMENT}[args.precision]
     if args.workload:
         cfg = workload_config(args.workload, precision=precision)
     else:
