@@ -49,7 +49,7 @@ struct SReq
   int                 steps = 0, steps_done = 0;
   double             *u = nullptr, *r = nullptr, *k = nullptr;
   double             *t0 = nullptr, *t1 = nullptr; // face traces (collocation groups)
-  int                 state = 0; // 0 queued, 1 active, 2 done, 3 failed
+  int                 state = 0; // 0 queued, 1 active, 2 done, 3 failed (device memory or launch at admission)
   double              t_submit = 0, t_admit = 0, t_done = 0, rel_l2 = -1;
   std::vector<double> solution;
   adv::DiagArgs       diag;
@@ -276,21 +276,37 @@ int admit(adv_server *S, int64_t id)
   SGroup *g = nullptr;
   if (int e = ensure_group(S, q.npts, q.precision, &g))
     return e;
-  const size_t nb = q.n_dofs * sizeof(double);
-  ADV_CUDA(cudaMallocAsync((void **)&q.u, nb, g->stream));
-  ADV_CUDA(cudaMallocAsync((void **)&q.r, nb, g->stream));
-  ADV_CUDA(cudaMallocAsync((void **)&q.k, nb, g->stream));
-  ADV_CUDA(adv::launch_project(q.diag, 0.0, q.u, g->stream));
-  ++S->launches;
-  if (adv::batch_collocation(q.precision))
+  const size_t    nb    = q.n_dofs * sizeof(double);
+  const bool      col   = adv::batch_collocation(q.precision);
+  const long long cells = (long long)q.n * q.n * q.n;
+  const size_t    tb    = (size_t)cells * 6 * q.npts * q.npts * sizeof(double);
+  cudaError_t     e     = cudaMallocAsync((void **)&q.u, nb, g->stream);
+  if (e == cudaSuccess)
+    e = cudaMallocAsync((void **)&q.r, nb, g->stream);
+  if (e == cudaSuccess)
+    e = cudaMallocAsync((void **)&q.k, nb, g->stream);
+  if (e == cudaSuccess && col)
+    e = cudaMallocAsync((void **)&q.t0, tb, g->stream);
+  if (e == cudaSuccess && col)
+    e = cudaMallocAsync((void **)&q.t1, tb, g->stream);
+  if (e == cudaSuccess)
+    e = adv::launch_project(q.diag, 0.0, q.u, g->stream);
+  if (e == cudaSuccess && col)
+    e = adv::launch_basis_change(q.npts, q.u, 0, cells, true, g->stream, q.t0);
+  if (e != cudaSuccess)
     {
-      const long long cells = (long long)q.n * q.n * q.n;
-      const size_t    tb    = (size_t)cells * 6 * q.npts * q.npts * sizeof(double);
-      ADV_CUDA(cudaMallocAsync((void **)&q.t0, tb, g->stream));
-      ADV_CUDA(cudaMallocAsync((void **)&q.t1, tb, g->stream));
-      ADV_CUDA(adv::launch_basis_change(q.npts, q.u, 0, cells, true, g->stream, q.t0));
-      ++S->launches;
+      // the request fails alone: give back what it holds, keep serving
+      cudaGetLastError();
+      for (double *p : {q.u, q.r, q.k, q.t0, q.t1})
+        if (p)
+          cudaFreeAsync(p, g->stream);
+      q.u = q.r = q.k = q.t0 = q.t1 = nullptr;
+      q.state  = 3;
+      q.t_done = now_s();
+      ++S->completed;
+      return ADV_OK;
     }
+  S->launches += col ? 2 : 1;
   q.state   = 1;
   q.t_admit = now_s();
   g->members.push_back(id);

@@ -29,7 +29,7 @@ from ._lib import IC_SINE_GAUSS, MESH_CARTESIAN, PRECISION_FP32_OPERATOR, PRECIS
 
 SIZES = (4, 6, 8, 12, 16, 24, 32)
 DEGREES = (2, 3, 4, 5, 6)
-STATE_QUEUED, STATE_RUNNING, STATE_DONE = 0, 1, 2
+STATE_QUEUED, STATE_RUNNING, STATE_DONE, STATE_FAILED = 0, 1, 2, 3
 
 
 @dataclass
@@ -197,7 +197,9 @@ def run_mix(requests, rate_clock=True, memory_budget_bytes=150 * 10 ** 9, steps_
         stats = srv.stats()
     lat = np.array([results[r.index]["latency_s"] for r in requests])
     work = sum(r.work() for r in requests)
-    summary = {"requests": len(requests), "wall_s": wall, "throughput_req_s": len(requests) / wall,
+    failed = sum(results[r.index]["state"] == STATE_FAILED for r in requests)
+    summary = {"requests": len(requests), "failed": int(failed), "wall_s": wall,
+               "throughput_req_s": len(requests) / wall,
                "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
                "gdof_stages_per_s": work / wall / 1e9, "ticks": stats["ticks"], "launches": stats["launches"],
                "max_rel_l2_error": max(results[r.index]["rel_l2_error"] for r in requests)}

@@ -257,7 +257,9 @@ int adv_server_submit(adv_server *s, const adv_config *cfg, double t_end, double
 int adv_server_poll(adv_server *s, int *n_completed);
 /* Polls until every submitted request is complete. */
 int adv_server_drain(adv_server *s);
-/* state: 0 queued, 1 running, 2 done; latency from submission to retirement. */
+/* state: 0 queued, 1 running, 2 done, 3 failed at admission (its device
+ * memory could not be allocated or its set-up launch failed; the server
+ * carries on with the other requests); latency from submission to retirement. */
 int adv_server_result(adv_server *s, int64_t request_id, int *state, double *rel_l2_error, double *latency_s,
                       int *steps, double *dt);
 /* Final solution of a done request (servers created with keep_solutions != 0). */
