@@ -103,13 +103,13 @@ def test_rejected_requests(cuda, adv_lib):
 
 
 def test_request_that_cannot_be_allocated_fails_alone(cuda, adv_lib):
-    """A request within the budget whose buffers exceed the device memory
-    (512^3 cells of degree 6, over 1 TB) fails at admission with state 3; the
-    other requests are served as usual."""
+    """A request within the budget whose buffers exceed the device memory by
+    far (1024^3 cells of degree 6: 2.9 TB per vector against 288 GB of HBM)
+    fails at admission with state 3; the other requests are served as usual."""
     from advection_miniapp_gb300.serving import STATE_DONE, STATE_FAILED, Request, Server
     small = Request(0, 3, 2, (1.0, 0.0, 0.0), (0.0, 0.0, 0.0), 0.05, 0)
-    huge = Request(1, 512, 6, (1.0, 0.0, 0.0), (0.0, 0.0, 0.0), 0.01, 0)
-    with Server(memory_budget_bytes=10 ** 13) as srv:
+    huge = Request(1, 1024, 6, (1.0, 0.0, 0.0), (0.0, 0.0, 0.0), 0.001, 0)
+    with Server(memory_budget_bytes=10 ** 14) as srv:
         ids = [srv.submit(small), srv.submit(huge), srv.submit(small)]
         srv.drain()
         states = [srv.result(i)["state"] for i in ids]
