@@ -125,6 +125,14 @@ int ensure_tables(int device)
         }
       if (n % 2)
         td[n].lwe[n / 2] = t.lw0[n / 2], tf[n].lwe[n / 2] = (float)t.lw0[n / 2];
+      for (int q = 0; q < n / 2; ++q)
+        {
+          const double e = 0.5 * (t.lwd0[q] + t.lwd0[n - 1 - q]), o = 0.5 * (t.lwd0[q] - t.lwd0[n - 1 - q]);
+          td[n].lde[q] = e, td[n].ldo[q] = o;
+          tf[n].lde[q] = (float)e, tf[n].ldo[q] = (float)o;
+        }
+      if (n % 2)
+        td[n].lde[n / 2] = t.lwd0[n / 2], tf[n].lde[n / 2] = (float)t.lwd0[n / 2];
       double Si[adv::kMaxN][adv::kMaxN] = {};
       for (int i = 0; i < n; ++i)
         for (int q = 0; q < n; ++q)
@@ -378,20 +386,25 @@ bool use_collocation(const adv_handle &h)
   return h.cfg.precision == ADV_PRECISION_FP64 || h.cfg.diffusion != 0.0;
 }
 
-// Face traces between the collocation stages: FP64 advection (SIPG needs
-// normal derivatives of the neighbours).  Measured on GB300 at degree 4, 64^3
+// Face traces between the collocation stages: FP64 (with SIPG they carry
+// the normal derivatives too).  Measured on GB300 at degree 4, 64^3
 // curved cells: FP64 13.4 vs 12.3 GDoF/s without; the FP32 operator got
 // slower with them (54.3 vs 61.0: one more barrier, more shared memory per
 // CTA), so it does not use them.
 bool use_traces(const adv_handle &h)
 {
-  return h.cfg.precision == ADV_PRECISION_FP64 && h.cfg.diffusion == 0.0 &&
-         h.cfg.fused_form != ADV_FORM_COLLOCATION_NO_TRACES;
+  return h.cfg.precision == ADV_PRECISION_FP64 && h.cfg.fused_form != ADV_FORM_COLLOCATION_NO_TRACES;
+}
+
+// trace values per face point: the value, and with SIPG its normal derivative
+int trace_width(const adv_handle &h)
+{
+  return h.cfg.diffusion != 0.0 ? 2 : 1;
 }
 
 int ensure_traces(adv_handle *h)
 {
-  const size_t nb = (size_t)h->mesh.n_cells * 6 * h->mesh.n * h->mesh.n * sizeof(double);
+  const size_t nb = (size_t)h->mesh.n_cells * 6 * trace_width(*h) * h->mesh.n * h->mesh.n * sizeof(double);
   for (int i = 0; i < 2; ++i)
     if (!h->d_traces[i])
       {
@@ -872,7 +885,7 @@ int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, 
   if (gauss)
     {
       ADV_CUDA(adv::launch_basis_change(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, true, s,
-                                        traces ? static_cast<double *>(tr_in) : nullptr));
+                                        traces ? static_cast<double *>(tr_in) : nullptr, trace_width(*h)));
       ++h->launches;
     }
   for (int step = 0; step < n_steps; ++step)

@@ -46,6 +46,10 @@ struct DevTables
   // lwe[q] = (lw0[q] + lw0[n-1-q]) / 2, lwo[q] = (lw0[q] - lw0[n-1-q]) / 2
   // for q < n/2, lwe[n/2] = lw0[n/2] for odd n
   T lwe[kMaxNDev], lwo[kMaxNDev];
+  // the same split of the derivative lifts (lwd1[q] = -lwd0[n-1-q]):
+  // lde[q] = (lwd0[q] + lwd0[n-1-q]) / 2, ldo[q] = (lwd0[q] - lwd0[n-1-q]) / 2,
+  // lde[n/2] = lwd0[n/2] for odd n
+  T lde[kMaxNDev], ldo[kMaxNDev];
 };
 
 // Index [n] holds the tables of n points per direction.  The library is

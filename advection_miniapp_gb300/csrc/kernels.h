@@ -86,9 +86,10 @@ cudaError_t upload_tables_gauss32(const DevTables<double> *d, const DevTables<fl
 // In-place change of basis of the cells [cell_begin, cell_end) of u:
 // to_gauss: Gauss-Lobatto nodal values -> values at the Gauss points (S x S x S);
 // otherwise the inverse (S^-1 x S^-1 x S^-1).  With traces (to_gauss only),
-// also writes the face traces of the result in the layout of StageArgs::tr_in.
+// also writes the face traces of the result in the layout of StageArgs::tr_in
+// (width 2: values and reference normal derivatives, for SIPG).
 cudaError_t launch_basis_change(int n, double *u, long long cell_begin, long long cell_end, bool to_gauss,
-                                cudaStream_t stream, double *traces = nullptr);
+                                cudaStream_t stream, double *traces = nullptr, int width = 1);
 // cells processed per CTA by the stage kernel (for launch accounting)
 int stage_cells_per_block(int n, int precision);
 

@@ -20,10 +20,11 @@
 // The fused LSRK loop changes the basis of the solution once on entry and
 // once on exit (launch_basis_change); the stages in between run here.
 //
-// Face traces (TR, FP64 advection): a stage also writes the values at the
-// face points of its output that the next stage reads (r_out, or u_out on a
-// last stage), [6][n^2] per cell; the next stage then reads its own and its
-// neighbours' face values instead of contracting pencils.  Per cell-stage at
+// Face traces (TR, FP64): a stage also writes the values at the face points
+// of its output that the next stage reads (r_out, or u_out on a last stage),
+// [6][n^2] per cell, and with SIPG also the reference normal derivatives
+// there ([6][2][n^2]); the next stage then reads its own and its neighbours'
+// face data instead of contracting pencils.  Per cell-stage at
 // degree 4 the producer adds 750 FMAs and the consumer saves 1500; the
 // traces are the same contractions in the same order, so results are
 // bit-identical to the variant without them.
@@ -41,7 +42,9 @@ struct GaussShape
   static constexpr int THREADS = SH::THREADS;
   // the nodal layout plus, with traces, Tb [C][6][NF] own face values,
   // padded to 16 bytes: the geometry after it is filled by 16-byte cp.async
-  static constexpr int TB_VALUES = TR ? (6 * C * N * N * (int)sizeof(T) + 15) / 16 * 16 / (int)sizeof(T) : 0;
+  // traces per face point: the value, and with SIPG the reference normal derivative
+  static constexpr int TRW       = VISC ? 2 : 1;
+  static constexpr int TB_VALUES = TR ? (TRW * 6 * C * N * N * (int)sizeof(T) + 15) / 16 * 16 / (int)sizeof(T) : 0;
   // field geometry with traces: the face coefficients are read from global
   // memory in the direction passes (one read per face point) instead of being
   // staged, which frees 12 C n^2 values of shared memory per CTA (one more
@@ -59,7 +62,6 @@ template <int N, typename T, bool UNI, bool VISC, bool TR = false>
 __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long long cell0,
                                                 unsigned char *smem_raw)
 {
-  static_assert(!(TR && VISC), "face traces carry values only, SIPG needs normal derivatives");
   using SH         = StageShape<N, T, UNI, VISC>;
   constexpr int C  = SH::C;
   constexpr int NQ = SH::NQ;
@@ -68,10 +70,11 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
   T   *Ub     = reinterpret_cast<T *>(smem_raw); // [C][NQ] Gauss-point values of r_in
   T   *Qb     = Ub + C * NQ;                     // [C][NQ] x and y contributions to Z
   T   *Nb     = Qb + C * NQ;                     // [C][6][NF] neighbour values at the face points
-  T   *Tb     = Nb + C * 6 * NF;                 // traces: [C][6][NF] own values at the face points
+  T   *Tb     = Nb + C * 6 * NF;                 // traces: [C][6][TRW][NF] own values (and derivatives)
   T   *Gb     = Tb + GaussShape<N, T, UNI, VISC, TR>::TB_VALUES; // field: [C][4][NQ] cell geometry
   using GS                 = GaussShape<N, T, UNI, VISC, TR>;
   constexpr bool FG        = GS::FACES_GLOBAL;
+  constexpr int  TRW       = GS::TRW;
   T   *Fb     = Gb + (UNI ? 0 : C * 4 * NQ);     // field: [C][6][2][NF] face coefficients (staged unless FG)
   T   *Nd     = Fb + GS::FB_VALUES;              // viscous: [C][6][NF] neighbour normal derivatives
   int *s_nbr  = reinterpret_cast<int *>(Nd + (VISC ? C * 6 * NF : 0));
@@ -105,8 +108,8 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
       Ub[i] = from_double<T>(__ldg(src + i));
     if (TR)
       {
-        const T *tr = static_cast<const T *>(A.tr_in) + cell0 * 6 * NF;
-        for (int i = tid; i < ncell * 6 * NF; i += NT)
+        const T *tr = static_cast<const T *>(A.tr_in) + cell0 * 6 * TRW * NF;
+        for (int i = tid; i < ncell * 6 * TRW * NF; i += NT)
           Tb[i] = __ldg(tr + i);
       }
   }
@@ -120,7 +123,10 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
           if (TR)
             {
               // the neighbour's own trace on the shared face (its face j ^ 1)
-              Nb[cf * NF + fq] = __ldg(static_cast<const T *>(A.tr_in) + ((long long)nb * 6 + (j ^ 1)) * NF + fq);
+              const T *tn      = static_cast<const T *>(A.tr_in) + ((long long)nb * 6 + (j ^ 1)) * TRW * NF + fq;
+              Nb[cf * NF + fq] = __ldg(tn);
+              if (VISC)
+                Nd[cf * NF + fq] = __ldg(tn + NF);
               continue;
             }
           // pencil of the neighbour along d through face point fq, contracted
@@ -173,13 +179,14 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
 #pragma unroll
       for (int k = 0; k < N; ++k)
         U[k] = p[k];
-      const T *Tr = Tb + cl * 6 * NF + r;
+      const T *Tr = Tb + cl * 6 * TRW * NF + r;
       direction_pass<N, T, UNI, VISC, 0, TR>(A, tb, U, Nb[(cl * 6 + 0) * NF + r], Nb[(cl * 6 + 1) * NF + r],
                                              VISC ? Nd[(cl * 6 + 0) * NF + r] : T(0),
                                              VISC ? Nd[(cl * 6 + 1) * NF + r] : T(0), s_nbr[cl * 6 + 0] < 0,
                                              s_nbr[cl * 6 + 1] < 0, r, faces(cl, 0), faces(cl, 1),
                                              Gb + cl * 4 * NQ + N * r,
-                                             1, out, TR ? Tr[0] : T(0), TR ? Tr[NF] : T(0));
+                                             1, out, TR ? Tr[0] : T(0), TR ? Tr[TRW * NF] : T(0),
+                                             TR && VISC ? Tr[NF] : T(0), TR && VISC ? Tr[TRW * NF + NF] : T(0));
       T *z = Qb + cl * NQ + N * r;
 #pragma unroll
       for (int k = 0; k < N; ++k)
@@ -197,13 +204,14 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
 #pragma unroll
       for (int k = 0; k < N; ++k)
         U[k] = p[k * N];
-      const T *Tr = Tb + cl * 6 * NF + 2 * NF + r;
+      const T *Tr = Tb + (cl * 6 + 2) * TRW * NF + r;
       direction_pass<N, T, UNI, VISC, 1, TR>(A, tb, U, Nb[(cl * 6 + 2) * NF + r], Nb[(cl * 6 + 3) * NF + r],
                                              VISC ? Nd[(cl * 6 + 2) * NF + r] : T(0),
                                              VISC ? Nd[(cl * 6 + 3) * NF + r] : T(0), s_nbr[cl * 6 + 2] < 0,
                                              s_nbr[cl * 6 + 3] < 0, r, faces(cl, 2), faces(cl, 3),
                                              Gb + (cl * 4 + 1) * NQ + off, N, out, TR ? Tr[0] : T(0),
-                                             TR ? Tr[NF] : T(0));
+                                             TR ? Tr[TRW * NF] : T(0), TR && VISC ? Tr[NF] : T(0),
+                                             TR && VISC ? Tr[TRW * NF + NF] : T(0));
       T *z = Qb + cl * NQ + off;
 #pragma unroll
       for (int k = 0; k < N; ++k)
@@ -222,13 +230,13 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
       for (int k = 0; k < N; ++k)
         U[k] = p[k * NF];
       const T *G  = Gb + cl * 4 * NQ;
-      const T *Tr = Tb + cl * 6 * NF + 4 * NF + r;
+      const T *Tr = Tb + (cl * 6 + 4) * TRW * NF + r;
       direction_pass<N, T, UNI, VISC, 2, TR>(A, tb, U, Nb[(cl * 6 + 4) * NF + r], Nb[(cl * 6 + 5) * NF + r],
                                              VISC ? Nd[(cl * 6 + 4) * NF + r] : T(0),
                                              VISC ? Nd[(cl * 6 + 5) * NF + r] : T(0), s_nbr[cl * 6 + 4] < 0,
                                              s_nbr[cl * 6 + 5] < 0, r, faces(cl, 4), faces(cl, 5), G + 2 * NQ + r,
-                                             NF, out,
-                                             TR ? Tr[0] : T(0), TR ? Tr[NF] : T(0));
+                                             NF, out, TR ? Tr[0] : T(0), TR ? Tr[TRW * NF] : T(0),
+                                             TR && VISC ? Tr[NF] : T(0), TR && VISC ? Tr[TRW * NF + NF] : T(0));
       T              *z  = Qb + cl * NQ + r;
       const long long gb = (cell0 + cl) * NQ + r;
       double          next[N]; // the next stage's input along the pencil (traces)
@@ -277,9 +285,15 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
           for (int k = 0; k < N; ++k)
             nt[k] = from_double<T>(next[k]);
           pencil_traces<N, T>(tb, nt, lo, hi);
-          T *to      = static_cast<T *>(A.tr_out) + (cell0 + cl) * 6 * NF + r;
-          to[4 * NF] = lo;
-          to[5 * NF] = hi;
+          T *to            = static_cast<T *>(A.tr_out) + ((cell0 + cl) * 6 + 4) * TRW * NF + r;
+          to[0]            = lo;
+          to[TRW * NF]     = hi;
+          if (VISC)
+            {
+              pencil_dtraces<N, T>(tb, nt, lo, hi);
+              to[NF]           = lo;
+              to[TRW * NF + NF] = hi;
+            }
 #pragma unroll
           for (int k = 0; k < N; ++k)
             z[k * NF] = nt[k];
@@ -300,9 +314,15 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
           for (int k = 0; k < N; ++k)
             x[k] = p[k * st];
           pencil_traces<N, T>(tb, x, lo, hi);
-          T *to  = static_cast<T *>(A.tr_out) + ((cell0 + cl) * 6 + 2 * dd) * NF + r;
-          to[0]  = lo;
-          to[NF] = hi;
+          T *to        = static_cast<T *>(A.tr_out) + ((cell0 + cl) * 6 + 2 * dd) * TRW * NF + r;
+          to[0]        = lo;
+          to[TRW * NF] = hi;
+          if (VISC)
+            {
+              pencil_dtraces<N, T>(tb, x, lo, hi);
+              to[NF]            = lo;
+              to[TRW * NF + NF] = hi;
+            }
         }
     }
 }
@@ -341,13 +361,14 @@ cudaError_t launch_stage_gauss_t(const StageArgs &args, cudaStream_t stream)
 template <int N, typename T>
 cudaError_t launch_stage_gauss_n(const StageArgs &args, cudaStream_t stream)
 {
-  if (args.visc)
-    return launch_stage_gauss_t<N, T, false, true, false>(args, stream);
   // face traces: FP64 only (the library's choice; the kernel code is generic)
   if constexpr (sizeof(T) == sizeof(double))
     if (args.tr_in)
-      return args.uniform ? launch_stage_gauss_t<N, T, true, false, true>(args, stream)
+      return args.visc ? launch_stage_gauss_t<N, T, false, true, true>(args, stream)
+           : args.uniform ? launch_stage_gauss_t<N, T, true, false, true>(args, stream)
                           : launch_stage_gauss_t<N, T, false, false, true>(args, stream);
+  if (args.visc)
+    return launch_stage_gauss_t<N, T, false, true, false>(args, stream);
   return args.uniform ? launch_stage_gauss_t<N, T, true, false, false>(args, stream)
                       : launch_stage_gauss_t<N, T, false, false, false>(args, stream);
 }

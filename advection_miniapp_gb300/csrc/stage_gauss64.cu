@@ -10,7 +10,7 @@ namespace
 // shared memory: one thread per pencil, C cells per CTA
 template <int N, bool TO_GAUSS>
 __global__ void __launch_bounds__(StageShape<N, double, true, false>::THREADS)
-  basis_kernel(double *u, long long cell_begin, long long cell_end, double *traces)
+  basis_kernel(double *u, long long cell_begin, long long cell_end, double *traces, int width)
 {
   using SH         = StageShape<N, double, true, false>;
   constexpr int C  = SH::C;
@@ -53,7 +53,8 @@ __global__ void __launch_bounds__(StageShape<N, double, true, false>::THREADS)
     g[i] = buf[i];
   if (TO_GAUSS && traces)
     {
-      // face traces of the result, [6][NF] per cell (StageArgs::tr_in)
+      // face traces of the result, [6][width][NF] per cell (StageArgs::tr_in):
+      // values, and with width 2 also reference normal derivatives
       for (int w = tid; w < 3 * ncell * NF; w += NT)
         {
           const int d = w / (ncell * NF), v = w % (ncell * NF);
@@ -65,25 +66,31 @@ __global__ void __launch_bounds__(StageShape<N, double, true, false>::THREADS)
           for (int k = 0; k < N; ++k)
             x[k] = buf[cl * NQ + off + k * st];
           pencil_traces<N, double>(tb, x, lo, hi);
-          double *to = traces + ((cell0 + cl) * 6 + 2 * d) * NF + r;
-          to[0]      = lo;
-          to[NF]     = hi;
+          double *to     = traces + ((cell0 + cl) * 6 + 2 * d) * width * NF + r;
+          to[0]          = lo;
+          to[width * NF] = hi;
+          if (width == 2)
+            {
+              pencil_dtraces<N, double>(tb, x, lo, hi);
+              to[NF]     = lo;
+              to[3 * NF] = hi;
+            }
         }
     }
 }
 
 template <int N>
 cudaError_t launch_basis_n(double *u, long long cell_begin, long long cell_end, bool to_gauss, cudaStream_t s,
-                           double *traces)
+                           double *traces, int width)
 {
   using SH               = StageShape<N, double, true, false>;
   const long long blocks = (cell_end - cell_begin + SH::C - 1) / SH::C;
   if (blocks <= 0)
     return cudaSuccess;
   if (to_gauss)
-    basis_kernel<N, true><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, traces);
+    basis_kernel<N, true><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, traces, width);
   else
-    basis_kernel<N, false><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, nullptr);
+    basis_kernel<N, false><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, nullptr, 1);
   return cudaGetLastError();
 }
 } // namespace
@@ -99,16 +106,16 @@ cudaError_t launch_stage_gauss_fp64(int n, const StageArgs &args, cudaStream_t s
 }
 
 cudaError_t launch_basis_change(int n, double *u, long long cell_begin, long long cell_end, bool to_gauss,
-                                cudaStream_t stream, double *traces)
+                                cudaStream_t stream, double *traces, int width)
 {
   switch (n)
     {
-      case 2: return launch_basis_n<2>(u, cell_begin, cell_end, to_gauss, stream, traces);
-      case 3: return launch_basis_n<3>(u, cell_begin, cell_end, to_gauss, stream, traces);
-      case 4: return launch_basis_n<4>(u, cell_begin, cell_end, to_gauss, stream, traces);
-      case 5: return launch_basis_n<5>(u, cell_begin, cell_end, to_gauss, stream, traces);
-      case 6: return launch_basis_n<6>(u, cell_begin, cell_end, to_gauss, stream, traces);
-      case 7: return launch_basis_n<7>(u, cell_begin, cell_end, to_gauss, stream, traces);
+      case 2: return launch_basis_n<2>(u, cell_begin, cell_end, to_gauss, stream, traces, width);
+      case 3: return launch_basis_n<3>(u, cell_begin, cell_end, to_gauss, stream, traces, width);
+      case 4: return launch_basis_n<4>(u, cell_begin, cell_end, to_gauss, stream, traces, width);
+      case 5: return launch_basis_n<5>(u, cell_begin, cell_end, to_gauss, stream, traces, width);
+      case 6: return launch_basis_n<6>(u, cell_begin, cell_end, to_gauss, stream, traces, width);
+      case 7: return launch_basis_n<7>(u, cell_begin, cell_end, to_gauss, stream, traces, width);
       default: return cudaErrorInvalidValue;
     }
 }

@@ -152,9 +152,13 @@ __device__ __forceinline__ void sweep_eo(const EvenOdd<T> &M, const T (&in)[N], 
 // odd halves: with ps = phlo + phhi, pd = phlo - phhi, the lift of point q is
 // lwe[q] ps + lwo[q] pd and of point n-1-q lwe[q] ps - lwo[q] pd, so the
 // pair costs two FMAs instead of four.
-template <int N, typename T>
+// DL adds the SIPG derivative lifts lwd0 dlo + lwd1 dhi the same way (by
+// the symmetry lwd1[q] = -lwd0[n-1-q]: lde[q] (dlo - dhi) + ldo[q] (dlo + dhi)
+// at q, lde[q] (dlo - dhi) - ldo[q] (dlo + dhi) at n-1-q).
+template <int N, typename T, bool DL = false>
 __device__ __forceinline__ void sweep_eo_anti_lift(const EvenOdd<T> &M, const T (&in)[N], T phlo, T phhi,
-                                                   const T *lwe, const T *lwo, T (&out)[N])
+                                                   const T *lwe, const T *lwo, T (&out)[N], T dlo = T(0),
+                                                   T dhi = T(0), const T *lde = nullptr, const T *ldo = nullptr)
 {
   constexpr int H = N / 2;
   T             e[H], o[H];
@@ -165,6 +169,7 @@ __device__ __forceinline__ void sweep_eo_anti_lift(const EvenOdd<T> &M, const T 
       o[i] = in[i] - in[N - 1 - i];
     }
   const T ps = phlo + phhi, pd = phlo - phhi;
+  const T ds = dlo - dhi, dd = dlo + dhi;
 #pragma unroll
   for (int q = 0; q < H; ++q)
     {
@@ -177,8 +182,13 @@ __device__ __forceinline__ void sweep_eo_anti_lift(const EvenOdd<T> &M, const T 
         }
       if (N % 2)
         E = fma(M.ce[q], in[H], E);
-      const T a      = fma(lwe[q], ps, O);
-      const T b      = fma(lwo[q], pd, E);
+      T a = fma(lwe[q], ps, O);
+      T b = fma(lwo[q], pd, E);
+      if (DL)
+        {
+          a = fma(lde[q], ds, a);
+          b = fma(ldo[q], dd, b);
+        }
       out[q]         = a + b;
       out[N - 1 - q] = a - b;
     }
@@ -188,7 +198,10 @@ __device__ __forceinline__ void sweep_eo_anti_lift(const EvenOdd<T> &M, const T 
 #pragma unroll
       for (int i = 1; i < H; ++i)
         m = fma(M.mid[i], o[i], m);
-      out[H] = fma(lwe[H], ps, m);
+      m = fma(lwe[H], ps, m);
+      if (DL)
+        m = fma(lde[H], ds, m);
+      out[H] = m;
     }
 }
 
@@ -224,12 +237,28 @@ __device__ __forceinline__ void pencil_traces(const DevTables<T> &tb, const T (&
     }
 }
 
-// OWN_TR: the own face values come precomputed (tr_lo, tr_hi)
+// The own reference normal derivatives at the faces of the pencil:
+// sum_q l'_q(0) U_q and sum_q l'_q(1) U_q.
+template <int N, typename T>
+__device__ __forceinline__ void pencil_dtraces(const DevTables<T> &tb, const T (&U)[N], T &dlo, T &dhi)
+{
+  dlo = tb.ld0[0] * U[0], dhi = tb.ld1[0] * U[0];
+#pragma unroll
+  for (int q = 1; q < N; ++q)
+    {
+      dlo = fma(tb.ld0[q], U[q], dlo);
+      dhi = fma(tb.ld1[q], U[q], dhi);
+    }
+}
+
+// OWN_TR: the own face values come precomputed (tr_lo, tr_hi), and with
+// VISC the own reference normal derivatives at the faces (dtr_lo, dtr_hi)
 template <int N, typename T, bool UNI, bool VISC, int D, bool OWN_TR = false>
 __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTables<T> &tb,
                                                const T (&U)[N], T nlo, T nhi, T dnlo, T dnhi, bool blo,
                                                bool bhi, int fq, const T *Flo, const T *Fhi, const T *vt,
-                                               int vstride, T (&out)[N], T tr_lo = T(0), T tr_hi = T(0))
+                                               int vstride, T (&out)[N], T tr_lo = T(0), T tr_hi = T(0),
+                                               T dtr_lo = T(0), T dtr_hi = T(0))
 {
   constexpr int NF = N * N;
   T             ulo, uhi;
@@ -301,6 +330,56 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
         }
       return;
     }
+  // SIPG face terms: value coefficients join the flux, normal-derivative
+  // coefficients are lifted with l'(s) / w
+  T dlo = T(0), dhi = T(0);
+  if (VISC)
+    {
+      T duo_lo, duo_hi;
+      if (OWN_TR)
+        duo_lo = dtr_lo, duo_hi = dtr_hi;
+      else
+        {
+          duo_lo = tb.ld0[0] * U[0], duo_hi = tb.ld1[0] * U[0];
+#pragma unroll
+          for (int q = 1; q < N; ++q)
+            {
+              duo_lo = fma(tb.ld0[q], U[q], duo_lo);
+              duo_hi = fma(tb.ld1[q], U[q], duo_hi);
+            }
+        }
+      const T un_lo  = blo ? T(2) * nlo - ulo : nlo;
+      const T un_hi  = bhi ? T(2) * nhi - uhi : nhi;
+      const T dun_lo = blo ? duo_lo : dnlo;
+      const T dun_hi = bhi ? duo_hi : dnhi;
+      const T K1 = Consts<T>::K1(A, D), K2 = Consts<T>::K2(A, D);
+      const T jl = un_lo - ulo, jh = uhi - un_hi; // jumps u- - u+ across the low / high face
+      phlo       = fma(K1, jl, fma(-K2, dun_lo + duo_lo, phlo));
+      phhi       = fma(-K1, jh, fma(K2, duo_hi + dun_hi, phhi));
+      dlo        = K2 * jl;
+      dhi        = K2 * jh;
+    }
+  if constexpr (VISC && N >= 5)
+    {
+      // (1 - skew) sa Dw (vt U) - nu Dw (D U) + lifts of values and
+      // derivatives on the even-odd recombination - skew sa vt D U
+      const T sk  = A.has_skew ? Consts<T>::skew(A) : T(0);
+      const T adv = (T(1) - sk) * sa;
+      const T cd  = Consts<T>::cdiff(A, D);
+      T       w[N], du[N];
+      sweep2<N, T, true>(tb.D, tb.D_eo, U, du);
+#pragma unroll
+      for (int q = 0; q < N; ++q)
+        w[q] = fma(adv, vt[q * vstride] * U[q], -cd * du[q]);
+      sweep_eo_anti_lift<N, T, true>(tb.Dw_eo, w, phlo, phhi, tb.lwe, tb.lwo, out, dlo, dhi, tb.lde, tb.ldo);
+      if (A.has_skew)
+        {
+#pragma unroll
+          for (int q = 0; q < N; ++q)
+            out[q] = fma(-sk * sa, vt[q * vstride] * du[q], out[q]);
+        }
+      return;
+    }
   T vtv[N], w[N], du[N];
   const bool need_du = VISC || A.has_skew;
   if (need_du)
@@ -322,29 +401,6 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
       for (int q = 0; q < N; ++q)
         out[q] = VISC ? fma(-sk * sa, vtv[q] * du[q], out[q])
                       : fma(T(1) - sk, out[q], -sk * (UNI ? du[q] : vtv[q] * du[q]));
-    }
-  // SIPG face terms: value coefficients join the flux, normal-derivative
-  // coefficients are lifted with l'(s) / w
-  T dlo = T(0), dhi = T(0);
-  if (VISC)
-    {
-      T duo_lo = tb.ld0[0] * U[0], duo_hi = tb.ld1[0] * U[0];
-#pragma unroll
-      for (int q = 1; q < N; ++q)
-        {
-          duo_lo = fma(tb.ld0[q], U[q], duo_lo);
-          duo_hi = fma(tb.ld1[q], U[q], duo_hi);
-        }
-      const T un_lo  = blo ? T(2) * nlo - ulo : nlo;
-      const T un_hi  = bhi ? T(2) * nhi - uhi : nhi;
-      const T dun_lo = blo ? duo_lo : dnlo;
-      const T dun_hi = bhi ? duo_hi : dnhi;
-      const T K1 = Consts<T>::K1(A, D), K2 = Consts<T>::K2(A, D);
-      const T jl = un_lo - ulo, jh = uhi - un_hi; // jumps u- - u+ across the low / high face
-      phlo       = fma(K1, jl, fma(-K2, dun_lo + duo_lo, phlo));
-      phhi       = fma(-K1, jh, fma(K2, duo_hi + dun_hi, phhi));
-      dlo        = K2 * jl;
-      dhi        = K2 * jh;
     }
   const T cv = Consts<T>::cv(A, D);
 #pragma unroll
