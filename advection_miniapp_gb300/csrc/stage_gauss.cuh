@@ -49,10 +49,16 @@ struct GaussShape
   // memory in the direction passes (one read per face point) instead of being
   // staged, which frees 12 C n^2 values of shared memory per CTA (one more
   // resident CTA per SM at degree 4)
-  static constexpr bool FACES_GLOBAL = TR && !UNI && !VISC;
+  // SIPG: the cell geometry and face coefficients are read from global
+  // memory too; staged they would take 4 C n^3 + 12 C n^2 values (at degree 5
+  // in FP64, 72 KB of a 145 KB CTA, one CTA per SM)
+  static constexpr bool GEO_GLOBAL   = VISC;
+  static constexpr bool FACES_GLOBAL = (TR && !UNI) || VISC;
   static constexpr int  FB_VALUES    = UNI || FACES_GLOBAL ? 0 : 12 * C * N * N;
+  static constexpr int  GB_VALUES    = UNI || GEO_GLOBAL ? 0 : 4 * C * N * N * N;
   static constexpr int  SMEM = SH::SMEM + TB_VALUES * (int)sizeof(T) -
-                              (UNI ? 0 : (12 * C * N * N - FB_VALUES) * (int)sizeof(T));
+                              (UNI ? 0 : (12 * C * N * N - FB_VALUES + 4 * C * N * N * N - GB_VALUES) *
+                                           (int)sizeof(T));
   // byte offset of the cell geometry Gb in the layout of stage_gauss_cta
   static constexpr int GB_OFFSET = (2 * C * N * N * N + 6 * C * N * N + TB_VALUES) * (int)sizeof(T);
   static_assert(GB_OFFSET % 16 == 0, "cp.async destinations need 16-byte alignment");
@@ -75,7 +81,7 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
   using GS                 = GaussShape<N, T, UNI, VISC, TR>;
   constexpr bool FG        = GS::FACES_GLOBAL;
   constexpr int  TRW       = GS::TRW;
-  T   *Fb     = Gb + (UNI ? 0 : C * 4 * NQ);     // field: [C][6][2][NF] face coefficients (staged unless FG)
+  T   *Fb     = Gb + GS::GB_VALUES;              // field: [C][6][2][NF] face coefficients (staged unless FG)
   T   *Nd     = Fb + GS::FB_VALUES;              // viscous: [C][6][NF] neighbour normal derivatives
   int *s_nbr  = reinterpret_cast<int *>(Nd + (VISC ? C * 6 * NF : 0));
   int *s_face = s_nbr + C * 6;
@@ -86,8 +92,14 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
 
   cell_neighbours(A, cell0, ncell, s_nbr, s_face, tid, NT);
   __syncthreads();
-  if (!UNI)
-    geometry_async<N, T>(A, cell0, ncell, s_face, Gb, Fb, tid, NT, !FG);
+  if (!UNI && !(GS::GEO_GLOBAL && FG))
+    geometry_async<N, T>(A, cell0, ncell, s_face, Gb, Fb, tid, NT, !FG, !GS::GEO_GLOBAL);
+  // cell geometry [vt0 | vt1 | vt2 | idet] of local cell cl: staged or global
+  auto geo = [&](int cl) -> const T * {
+    if (GS::GEO_GLOBAL)
+      return static_cast<const T *>(A.cell_geo) + (cell0 + cl) * 4 * NQ;
+    return Gb + cl * 4 * NQ;
+  };
 
   // face coefficients [P | M] of face j of local cell cl: staged or global
   auto faces = [&](int cl, int j) -> const T * {
@@ -184,7 +196,7 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
                                              VISC ? Nd[(cl * 6 + 0) * NF + r] : T(0),
                                              VISC ? Nd[(cl * 6 + 1) * NF + r] : T(0), s_nbr[cl * 6 + 0] < 0,
                                              s_nbr[cl * 6 + 1] < 0, r, faces(cl, 0), faces(cl, 1),
-                                             Gb + cl * 4 * NQ + N * r,
+                                             geo(cl) + N * r,
                                              1, out, TR ? Tr[0] : T(0), TR ? Tr[TRW * NF] : T(0),
                                              TR && VISC ? Tr[NF] : T(0), TR && VISC ? Tr[TRW * NF + NF] : T(0));
       T *z = Qb + cl * NQ + N * r;
@@ -209,7 +221,7 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
                                              VISC ? Nd[(cl * 6 + 2) * NF + r] : T(0),
                                              VISC ? Nd[(cl * 6 + 3) * NF + r] : T(0), s_nbr[cl * 6 + 2] < 0,
                                              s_nbr[cl * 6 + 3] < 0, r, faces(cl, 2), faces(cl, 3),
-                                             Gb + (cl * 4 + 1) * NQ + off, N, out, TR ? Tr[0] : T(0),
+                                             geo(cl) + NQ + off, N, out, TR ? Tr[0] : T(0),
                                              TR ? Tr[TRW * NF] : T(0), TR && VISC ? Tr[NF] : T(0),
                                              TR && VISC ? Tr[TRW * NF + NF] : T(0));
       T *z = Qb + cl * NQ + off;
@@ -229,7 +241,7 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
 #pragma unroll
       for (int k = 0; k < N; ++k)
         U[k] = p[k * NF];
-      const T *G  = Gb + cl * 4 * NQ;
+      const T *G  = geo(cl);
       const T *Tr = Tb + (cl * 6 + 4) * TRW * NF + r;
       direction_pass<N, T, UNI, VISC, 2, TR>(A, tb, U, Nb[(cl * 6 + 4) * NF + r], Nb[(cl * 6 + 5) * NF + r],
                                              VISC ? Nd[(cl * 6 + 4) * NF + r] : T(0),

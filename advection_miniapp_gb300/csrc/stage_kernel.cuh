@@ -460,12 +460,13 @@ __device__ __forceinline__ void cell_neighbours(const StageArgs &A, long long ce
 // group; the caller waits with __pipeline_wait_prior(0) before using them.
 template <int N, typename T>
 __device__ __forceinline__ void geometry_async(const StageArgs &A, long long cell0, int ncell, const int *s_face,
-                                               T *Gb, T *Fb, int tid, int nthreads, bool faces = true)
+                                               T *Gb, T *Fb, int tid, int nthreads, bool faces = true,
+                                               bool cells = true)
 {
   constexpr int NQ  = N * N * N;
   constexpr int NF  = N * N;
   const char   *geo = reinterpret_cast<const char *>(static_cast<const T *>(A.cell_geo) + cell0 * 4 * NQ);
-  const int     n16 = ncell * 4 * NQ * (int)sizeof(T) / 16;
+  const int     n16 = cells ? ncell * 4 * NQ * (int)sizeof(T) / 16 : 0;
   for (int i = tid; i < n16; i += nthreads)
     __pipeline_memcpy_async(reinterpret_cast<char *>(Gb) + 16 * i, geo + 16 * i, 16);
   constexpr int F8 = 2 * NF * (int)sizeof(T) / 8; // 8-byte chunks per cell-face
