@@ -51,7 +51,10 @@ struct GaussShape
   // resident CTA per SM at degree 4)
   // SIPG: the cell geometry and face coefficients are read from global
   // memory too; staged they would take 4 C n^3 + 12 C n^2 values (at degree 5
-  // in FP64, 72 KB of a 145 KB CTA, one CTA per SM)
+  // in FP64, 72 KB of a 145 KB CTA, one CTA per SM).  Measured on GB300: the
+  // degree-5 SIPG workload gains 15 % (FP64) and 19 % (FP32); the advection
+  // kernels lose 7 % (FP64) and 4 % (FP32) with global geometry, so they keep
+  // staging it.
   static constexpr bool GEO_GLOBAL   = VISC;
   static constexpr bool FACES_GLOBAL = (TR && !UNI) || VISC;
   static constexpr int  FB_VALUES    = UNI || FACES_GLOBAL ? 0 : 12 * C * N * N;
