@@ -93,6 +93,7 @@ SIGNATURES = {
     "adv_load_state": (_I, [_P, _P, _DP, ctypes.c_char_p, _P]),
     "adv_server_create": (_I, [_I64, _I, _I, _I, ctypes.POINTER(_P)]),
     "adv_server_destroy": (_I, [_P]),
+    "adv_server_set_policy": (_I, [_P, _I]),
     "adv_server_submit": (_I, [_P, ctypes.POINTER(AdvConfig), _D, _D, ctypes.POINTER(_I64)]),
     "adv_server_poll": (_I, [_P, ctypes.POINTER(_I)]),
     "adv_server_drain": (_I, [_P]),

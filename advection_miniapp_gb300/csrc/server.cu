@@ -85,6 +85,7 @@ struct adv_server
   int64_t             completed = 0, ticks = 0, launches = 0;
   std::map<int, SGroup> groups; // key: npts * 2 + precision
   int                 device = 0;
+  int                 policy = ADV_SERVE_FIFO;
 };
 
 namespace
@@ -338,6 +339,14 @@ int adv_server_create(int64_t memory_budget_bytes, int steps_per_tick, int max_a
   return ADV_OK;
 }
 
+int adv_server_set_policy(adv_server *S, int policy)
+{
+  if (!S || (policy != ADV_SERVE_FIFO && policy != ADV_SERVE_SHORTEST_FIRST))
+    return fail(ADV_ERR_INVALID, "unknown admission policy");
+  S->policy = policy;
+  return ADV_OK;
+}
+
 int adv_server_destroy(adv_server *S)
 {
   if (!S)
@@ -473,10 +482,21 @@ int adv_server_poll(adv_server *S, int *n_completed)
     }
   while (!S->queue.empty() && S->active < S->max_active)
     {
-      const int64_t id = S->queue.front();
+      auto pick = S->queue.begin();
+      if (S->policy == ADV_SERVE_SHORTEST_FIRST)
+        {
+          // the queued request with the least work (DoFs x steps)
+          for (auto it = S->queue.begin(); it != S->queue.end(); ++it)
+            {
+              const SReq &a = S->reqs[*it], &b = S->reqs[*pick];
+              if ((double)a.n_dofs * a.steps < (double)b.n_dofs * b.steps)
+                pick = it;
+            }
+        }
+      const int64_t id = *pick;
       if (S->used + S->reqs[id].bytes > S->budget)
         break;
-      S->queue.pop_front();
+      S->queue.erase(pick);
       if (int e = admit(S, id))
         return e;
     }

@@ -30,6 +30,7 @@ from ._lib import IC_SINE_GAUSS, MESH_CARTESIAN, PRECISION_FP32_OPERATOR, PRECIS
 SIZES = (4, 6, 8, 12, 16, 24, 32)
 DEGREES = (2, 3, 4, 5, 6)
 STATE_QUEUED, STATE_RUNNING, STATE_DONE, STATE_FAILED = 0, 1, 2, 3
+POLICIES = {"fifo": 0, "shortest": 1}
 
 
 @dataclass
@@ -101,7 +102,8 @@ def request_mix(n_requests, seed=0, rate=None, sizes=SIZES, degrees=DEGREES, t_r
 class Server:
     """Python face of adv_server (not thread-safe, like the C object)."""
 
-    def __init__(self, memory_budget_bytes=150 * 10 ** 9, steps_per_tick=8, max_active=4096, keep_solutions=False):
+    def __init__(self, memory_budget_bytes=150 * 10 ** 9, steps_per_tick=8, max_active=4096, keep_solutions=False,
+                 policy="fifo"):
         import torch
         torch.cuda.init()
         self._lib = _lib.load()
@@ -109,6 +111,7 @@ class Server:
         _lib.check(self._lib.adv_server_create(int(memory_budget_bytes), steps_per_tick, max_active,
                                                1 if keep_solutions else 0, ctypes.byref(self._s)),
                    "adv_server_create")
+        _lib.check(self._lib.adv_server_set_policy(self._s, POLICIES[policy]), "adv_server_set_policy")
 
     def close(self):
         if getattr(self, "_s", None):
@@ -166,13 +169,13 @@ class Server:
 
 
 def run_mix(requests, rate_clock=True, memory_budget_bytes=150 * 10 ** 9, steps_per_tick=8, max_active=4096,
-            keep_solutions=False):
+            keep_solutions=False, policy="fifo"):
     """Drive a server with the request stream: each request is submitted
     when the wall clock passes its arrival time (all at once without
     rate_clock).  Returns (results, summary, server solutions or None)."""
     import torch
     order = sorted(requests, key=lambda r: r.arrival)
-    with Server(memory_budget_bytes, steps_per_tick, max_active, keep_solutions) as srv:
+    with Server(memory_budget_bytes, steps_per_tick, max_active, keep_solutions, policy) as srv:
         ids = {}
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -250,13 +253,16 @@ def main(argv=None):
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--budget-gb", type=float, default=150.0)
     p.add_argument("--steps-per-tick", type=int, default=8)
+    p.add_argument("--max-active", type=int, default=4096, help="solves on the device at once")
+    p.add_argument("--policy", choices=sorted(POLICIES), default="fifo", help="admission order")
     p.add_argument("--t-max", type=float, default=1.0, help="upper end of the end-time range [0.1, t_max]")
     p.add_argument("--baseline", action="store_true", help="also run the requests one at a time")
     args = p.parse_args(argv)
     reqs = request_mix(args.requests, args.seed, args.rate or None, t_range=(0.1, args.t_max))
     _, summary, _ = run_mix(reqs, rate_clock=bool(args.rate), memory_budget_bytes=int(args.budget_gb * 1e9),
-                            steps_per_tick=args.steps_per_tick)
-    out = {"rate_req_s": args.rate, "seed": args.seed, "t_range": [0.1, args.t_max], "serving": summary}
+                            steps_per_tick=args.steps_per_tick, max_active=args.max_active, policy=args.policy)
+    out = {"rate_req_s": args.rate, "seed": args.seed, "t_range": [0.1, args.t_max], "policy": args.policy,
+           "max_active": args.max_active, "serving": summary}
     if args.baseline:
         _, base = run_one_at_a_time(reqs, rate_clock=bool(args.rate))
         out["one_at_a_time"] = base

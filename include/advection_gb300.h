@@ -249,6 +249,11 @@ typedef struct adv_server adv_server;
 int adv_server_create(int64_t memory_budget_bytes, int steps_per_tick, int max_active, int keep_solutions,
                       adv_server **out);
 int adv_server_destroy(adv_server *s);
+/* Admission order: FIFO (default), or the queued request with the least work
+ * (DoFs x steps) first; with max_active below the queue length the latter
+ * lets short solves overtake long ones (lower median latency, longer tail). */
+enum { ADV_SERVE_FIFO = 0, ADV_SERVE_SHORTEST_FIRST = 1 };
+int adv_server_set_policy(adv_server *s, int policy);
 /* Queues a solve of cfg (its initial condition) to t_end. */
 int adv_server_submit(adv_server *s, const adv_config *cfg, double t_end, double courant, int64_t *request_id);
 /* One scheduling round (non-blocking on the GPU): retire finished solves

@@ -115,3 +115,18 @@ def test_request_that_cannot_be_allocated_fails_alone(cuda, adv_lib):
         states = [srv.result(i)["state"] for i in ids]
         assert states == [STATE_DONE, STATE_FAILED, STATE_DONE]
         assert srv.stats()["device_bytes"] == 0 and srv.stats()["completed"] == 3
+
+
+def test_shortest_first_policy_same_results(cuda, adv_lib):
+    """Admission order changes latency, not results: shortest-first with a
+    small concurrency cap gives the FIFO results bit for bit, and finishes
+    the smallest request before the largest."""
+    from advection_miniapp_gb300.serving import run_mix
+    reqs = small_mix(seed=9, n=12)
+    res_f, _, sol_f = run_mix(reqs, rate_clock=False, keep_solutions=True)
+    res_s, _, sol_s = run_mix(reqs, rate_clock=False, keep_solutions=True, policy="shortest", max_active=2)
+    for r in reqs:
+        np.testing.assert_array_equal(sol_f[r.index], sol_s[r.index])
+    work = {r.index: r.work() for r in reqs}
+    small, big = min(work, key=work.get), max(work, key=work.get)
+    assert res_s[small]["latency_s"] < res_s[big]["latency_s"]
