@@ -355,41 +355,70 @@ __global__ void __launch_bounds__(kVecThreads)
   multi_dot_kernel(const double *__restrict__ V, long long ld, int m, const double *__restrict__ w, long long n,
                    double *partials)
 {
-  __shared__ double red[kVecThreads / 32];
+  // partial sums of <V_i, w> over this block's chunk: up to 8 products per
+  // pass kept in registers, so each vector element is read once and w once
+  // per pass; then one block reduction per pass
+  constexpr int     G = 8;
+  __shared__ double red[G][kVecThreads / 32];
   const long long   chunk = (n + gridDim.x - 1) / gridDim.x;
   const long long   lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
-  for (int i = 0; i < m; ++i)
+  const int         lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+  for (int i0 = 0; i0 < m; i0 += G)
     {
-      const double *v = V + i * ld;
-      double        s = 0.0;
+      const int g = min(G, m - i0);
+      double    s[G];
+#pragma unroll
+      for (int j = 0; j < G; ++j)
+        s[j] = 0.0;
       for (long long e = lo + threadIdx.x; e < hi; e += blockDim.x)
-        s = fma(__ldg(v + e), __ldg(w + e), s);
-      for (int o = 16; o > 0; o >>= 1)
-        s += __shfl_down_sync(0xffffffffu, s, o);
-      if (threadIdx.x % 32 == 0)
-        red[threadIdx.x / 32] = s;
+        {
+          const double we = __ldg(w + e);
+#pragma unroll
+          for (int j = 0; j < G; ++j)
+            if (j < g)
+              s[j] = fma(__ldg(V + (i0 + j) * ld + e), we, s[j]);
+        }
+#pragma unroll
+      for (int j = 0; j < G; ++j)
+        {
+          for (int o = 16; o > 0; o >>= 1)
+            s[j] += __shfl_down_sync(0xffffffffu, s[j], o);
+          if (lane == 0)
+            red[j][warp] = s[j];
+        }
       __syncthreads();
-      if (threadIdx.x == 0)
+      if (threadIdx.x < g)
         {
           double t = 0.0;
           for (int k = 0; k < kVecThreads / 32; ++k)
-            t += red[k];
-          partials[blockIdx.x * m + i] = t;
+            t += red[threadIdx.x][k];
+          partials[blockIdx.x * m + i0 + threadIdx.x] = t;
         }
       __syncthreads();
     }
 }
 
-// out[i] = sum_b partials[b * m + i], one thread per i, fixed order
-__global__ void reduce_partials_kernel(const double *partials, int blocks, int m, double *out)
+// out[i] = sum_b partials[b * m + i]: block i, strided partial sums per
+// thread and a tree over the threads (a fixed order, so results repeat)
+__global__ void __launch_bounds__(kVecThreads) reduce_partials_kernel(const double *partials, int blocks, int m,
+                                                                      double *out)
 {
-  const int i = threadIdx.x;
-  if (i < m)
+  __shared__ double red[kVecThreads / 32];
+  const int         i = blockIdx.x;
+  double            s = 0.0;
+  for (int b = threadIdx.x; b < blocks; b += blockDim.x)
+    s += partials[b * m + i];
+  for (int o = 16; o > 0; o >>= 1)
+    s += __shfl_down_sync(0xffffffffu, s, o);
+  if (threadIdx.x % 32 == 0)
+    red[threadIdx.x / 32] = s;
+  __syncthreads();
+  if (threadIdx.x == 0)
     {
-      double s = 0.0;
-      for (int b = 0; b < blocks; ++b)
-        s += partials[b * m + i];
-      out[i] = s;
+      double t = 0.0;
+      for (int k = 0; k < kVecThreads / 32; ++k)
+        t += red[k];
+      out[i] = t;
     }
 }
 
@@ -493,7 +522,7 @@ cudaError_t launch_multi_dot(const double *V, long long ld, int m, const double 
 {
   const int blocks = vec_blocks(n);
   multi_dot_kernel<<<blocks, kVecThreads, 0, s>>>(V, ld, m, w, n, partials);
-  reduce_partials_kernel<<<1, 64, 0, s>>>(partials, blocks, m, out);
+  reduce_partials_kernel<<<m, kVecThreads, 0, s>>>(partials, blocks, m, out);
   return cudaGetLastError();
 }
 
