@@ -93,6 +93,19 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
   const int           tid   = threadIdx.x;
   const int           ncell = (int)min((long long)C, A.n_cells - cell0);
 
+  // binary32 operator: ask L2 for the CTA's ranges of u_in and k_add, read
+  // by the update after the three passes
+  if (sizeof(T) == sizeof(float) && (A.mode == kModeStage || A.mode == kModeLastStage))
+    {
+      const int lines = (ncell * NQ * (int)sizeof(double) + 127) / 128;
+      for (int i = tid; i < 2 * lines; i += NT)
+        {
+          const double *base = i < lines ? A.u_in : A.k_add;
+          if (base)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(reinterpret_cast<const char *>(base + cell0 * NQ) +
+                                                          128 * (i % lines)));
+        }
+    }
   cell_neighbours(A, cell0, ncell, s_nbr, s_face, tid, NT);
   __syncthreads();
   if (!UNI && !(GS::GEO_GLOBAL && FG))

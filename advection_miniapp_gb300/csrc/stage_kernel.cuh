@@ -505,7 +505,16 @@ __device__ __forceinline__ void stage_cta(const StageArgs &A, const long long ce
   const int           tid   = threadIdx.x;
   const int           ncell = (int)min((long long)C, A.n_cells - cell0);
 
-  // ---- phase 0a: neighbour cells and face ids of the CTA's cells
+  // ---- phase 0a: neighbour cells and face ids of the CTA's cells; the
+  //      binary32 operator also asks L2 for the CTA's range of u_in, which
+  //      the update reads only after the seven barriers of the stage
+  if (sizeof(T) == sizeof(float) && A.u_in && (A.mode == kModeStage || A.mode == kModeLastStage))
+    {
+      const char *ub    = reinterpret_cast<const char *>(A.u_in + cell0 * NQ);
+      const int   lines = (ncell * NQ * (int)sizeof(double) + 127) / 128;
+      for (int i = tid; i < lines; i += NT)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(ub + 128 * i));
+    }
   cell_neighbours(A, cell0, ncell, s_nbr, s_face, tid, NT);
   __syncthreads();
 
