@@ -63,6 +63,8 @@ def test_default_config(adv_lib):
     dict(mesh_type=5), dict(mesh_type=1, deformation=0.5), dict(velocity_type=3),
     dict(velocity_type=1, velocity_period=0.0), dict(precision=7), dict(initial_condition=9),
     dict(initial_condition=1, ic_params=(0.5, 0.5, 0.5, 0.0)), dict(flux_alpha=2.0),
+    dict(fused_form=9), dict(diffusion=-1.0), dict(diffusion=1e-3, mesh_type=1, deformation=0.05),
+    dict(diffusion=1e-3, penalty_factor=0.0),
 ])
 def test_invalid_configs_rejected_on_host(adv_lib, bad):
     from advection_miniapp_gb300 import _lib
@@ -92,3 +94,21 @@ def test_lsrk_coefficients_match_oracle(adv_lib, oracle_mod):
         np.testing.assert_array_equal(b, bo)
     from advection_miniapp_gb300 import _lib
     assert _lib.load().adv_lsrk_coefficients(9, None, None, None) == 1
+
+
+def test_host_only_entry_points_reject_bad_input(adv_lib):
+    """Slab layouts and the serving loop check their arguments before any
+    device work."""
+    from advection_miniapp_gb300 import _lib
+    L = _lib.load()
+    c = adv_lib.make_config(n_cells=(4, 4, 6))
+    out = (ctypes.c_int64 * 10)()
+    for zb, ze in ((-1, 3), (2, 2), (3, 7)):
+        assert L.adv_slab_layout(ctypes.byref(c), zb, ze, out) == 1
+    assert L.adv_slab_layout(ctypes.byref(c), 0, 6, out) == 0 and out[8] == 8  # periodic: two ghost layers
+    s = ctypes.c_void_p()
+    assert L.adv_server_create(0, 8, 16, 0, ctypes.byref(s)) == 1
+    assert L.adv_server_create(1 << 30, 0, 16, 0, ctypes.byref(s)) == 1
+    assert L.adv_server_create(1 << 30, 8, 0, 0, ctypes.byref(s)) == 1
+    assert L.adv_server_set_policy(None, 0) == 1
+    assert L.adv_write_vtu_host(ctypes.byref(adv_lib.make_config(degree=0)), None, 0.0, b"x.vtu") == 1
