@@ -215,6 +215,16 @@ class AdvectionOperation:
         _lib.check(self._lib.adv_apply_mass(self._h, self._ptr(src), self._ptr(dst), _stream_handle(stream)),
                    "adv_apply_mass")
 
+    # -- timing (computing_times, advection_solver.cc:349-372) -------------
+    def set_timing(self, enable=True):
+        _lib.check(self._lib.adv_set_timing(self._h, 1 if enable else 0), "adv_set_timing")
+
+    def timing(self):
+        """(device seconds, calls) accumulated by the timed calls so far."""
+        sec, calls = ctypes.c_double(), ctypes.c_int64()
+        _lib.check(self._lib.adv_timing(self._h, ctypes.byref(sec), ctypes.byref(calls)), "adv_timing")
+        return sec.value, calls.value
+
     # -- output (advection_solver.cc:1220-1241) -----------------------------
     def write_vtu(self, vec, time, path, stream=None):
         """VTU file with "solution" and "analytic_solution" at the support points."""

@@ -87,6 +87,8 @@ SIGNATURES = {
     "adv_bdf2_step": (_I, [_P, _D, _D, _I, _P, _P, _P, _D, ctypes.POINTER(_I), _P]),
     "adv_create_slab": (_I, [ctypes.POINTER(AdvConfig), _I, _I, ctypes.POINTER(_P)]),
     "adv_slab_layout": (_I, [ctypes.POINTER(AdvConfig), _I, _I, ctypes.POINTER(_I64)]),
+    "adv_set_timing": (_I, [_P, _I]),
+    "adv_timing": (_I, [_P, _DP, ctypes.POINTER(_I64)]),
     "adv_write_vtu": (_I, [_P, _P, _D, ctypes.c_char_p, _P]),
     "adv_write_vtu_host": (_I, [ctypes.POINTER(AdvConfig), _DP, _D, ctypes.c_char_p]),
     "adv_save_state": (_I, [_P, _P, _D, ctypes.c_char_p, _P]),
@@ -97,6 +99,7 @@ SIGNATURES = {
     "adv_server_submit": (_I, [_P, ctypes.POINTER(AdvConfig), _D, _D, ctypes.POINTER(_I64)]),
     "adv_server_poll": (_I, [_P, ctypes.POINTER(_I)]),
     "adv_server_drain": (_I, [_P]),
+    "adv_server_cancel": (_I, [_P, _I64]),
     "adv_server_result": (_I, [_P, _I64, ctypes.POINTER(_I), _DP, _DP, ctypes.POINTER(_I), _DP]),
     "adv_server_solution": (_I, [_P, _I64, _DP, _I64]),
     "adv_server_stats": (_I, [_P, ctypes.POINTER(_I64)]),

@@ -6,6 +6,7 @@
 // buffer rotation that lets every fused stage kernel read r_in while writing
 // its outputs to other buffers.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cmath>
 #include <cstdio>
@@ -438,6 +439,38 @@ namespace adv
 {
 namespace detail
 {
+CallTrace::CallTrace(adv_handle *h, const char *name, cudaStream_t s) : h_(h), s_(s)
+{
+  nvtxRangePushA(name);
+  // only the outermost traced call of a handle is timed (fgmres calls the
+  // preconditioner, a BDF2 step calls fgmres)
+  const bool outer = h_ && h_->trace_depth++ == 0;
+  if (outer && h_->timing && cudaEventCreate(&e0_) == cudaSuccess && cudaEventRecord(e0_, s_) != cudaSuccess)
+    {
+      cudaEventDestroy(e0_);
+      e0_ = nullptr;
+    }
+}
+
+CallTrace::~CallTrace()
+{
+  if (e0_)
+    {
+      cudaEvent_t e1 = nullptr;
+      if (cudaEventCreate(&e1) == cudaSuccess && cudaEventRecord(e1, s_) == cudaSuccess)
+        h_->timed_events.emplace_back(e0_, e1);
+      else
+        {
+          cudaEventDestroy(e0_);
+          if (e1)
+            cudaEventDestroy(e1);
+        }
+    }
+  if (h_)
+    --h_->trace_depth;
+  nvtxRangePop();
+}
+
 adv::StageArgs base_args(const adv_handle &h, double t, int op_precision) { return ::base_args(h, t, op_precision); }
 int            launch(adv_handle *h, const adv::StageArgs &A, cudaStream_t s) { return ::launch(h, A, s); }
 int            check_device(const adv_handle *h) { return ::check_device(h); }
@@ -598,6 +631,36 @@ int adv_slab_layout(const adv_config *cfg, int z_begin, int z_end, int64_t *out)
   return ADV_OK;
 }
 
+int adv_set_timing(adv_handle *h, int enable)
+{
+  if (!h)
+    return fail(ADV_ERR_INVALID, "null argument");
+  h->timing = enable != 0;
+  return ADV_OK;
+}
+
+int adv_timing(adv_handle *h, double *seconds, int64_t *calls)
+{
+  if (!h)
+    return fail(ADV_ERR_INVALID, "null argument");
+  for (auto &p : h->timed_events)
+    {
+      float ms = 0.0f;
+      ADV_CUDA(cudaEventSynchronize(p.second));
+      ADV_CUDA(cudaEventElapsedTime(&ms, p.first, p.second));
+      h->timed_seconds += 1e-3 * ms;
+      ++h->timed_calls;
+      cudaEventDestroy(p.first);
+      cudaEventDestroy(p.second);
+    }
+  h->timed_events.clear();
+  if (seconds)
+    *seconds = h->timed_seconds;
+  if (calls)
+    *calls = h->timed_calls;
+  return ADV_OK;
+}
+
 int adv_destroy(adv_handle *h)
 {
   if (!h)
@@ -616,6 +679,11 @@ int adv_destroy(adv_handle *h)
   cudaFree(h->d_fdm_cell_f);
   cudaFree(h->d_scratch[0]);
   cudaFree(h->d_scratch[1]);
+  for (auto &p : h->timed_events)
+    {
+      cudaEventDestroy(p.first);
+      cudaEventDestroy(p.second);
+    }
   cudaFree(h->d_traces[0]);
   cudaFree(h->d_traces[1]);
   delete h;
@@ -673,6 +741,7 @@ int adv_free_vector(adv_handle *h, double *vec)
 
 int adv_apply(adv_handle *h, const double *src, double *dst, double t, void *stream)
 {
+  adv::detail::CallTrace trace_(h, "adv_apply", (cudaStream_t)stream);
   if (!h || !src || !dst)
     return fail(ADV_ERR_INVALID, "null argument");
   if (int e = check_device(h))
@@ -699,6 +768,7 @@ int adv_apply(adv_handle *h, const double *src, double *dst, double t, void *str
 int adv_perform_stage(adv_handle *h, double t, double b_dt, double a_dt, const double *r_in,
                       double *k, double *u, double *r_out, void *stream)
 {
+  adv::detail::CallTrace trace_(h, "adv_perform_stage", (cudaStream_t)stream);
   if (!h || !r_in || !u || (a_dt != 0.0 && !r_out))
     return fail(ADV_ERR_INVALID, "null argument");
   if (a_dt != 0.0 && r_out == u)
@@ -854,6 +924,7 @@ bool increment_form_applies(const adv_handle &h)
 int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, double *u, double *r,
                    double *k, void *stream)
 {
+  adv::detail::CallTrace trace_(h, "adv_lsrk_steps", (cudaStream_t)stream);
   if (!h || !u || !r || !k)
     return fail(ADV_ERR_INVALID, "null argument");
   if (u == r || u == k || r == k)
@@ -947,6 +1018,7 @@ int adv_lsrk_step(adv_handle *h, int scheme, double t, double dt, double *u, dou
 
 int adv_project(adv_handle *h, double t, double *dst, void *stream)
 {
+  adv::detail::CallTrace trace_(h, "adv_project", (cudaStream_t)stream);
   if (!h || !dst)
     return fail(ADV_ERR_INVALID, "null argument");
   if (int e = check_device(h))
@@ -958,6 +1030,7 @@ int adv_project(adv_handle *h, double t, double *dst, void *stream)
 
 int adv_mass_energy(adv_handle *h, const double *u, double out[3], void *stream)
 {
+  adv::detail::CallTrace trace_(h, "adv_mass_energy", (cudaStream_t)stream);
   if (!h || !u || !out)
     return fail(ADV_ERR_INVALID, "null argument");
   if (int e = check_device(h))
@@ -978,6 +1051,7 @@ int adv_mass_energy(adv_handle *h, const double *u, double out[3], void *stream)
 
 int adv_l2_error(adv_handle *h, const double *u, double t, double out[2], void *stream)
 {
+  adv::detail::CallTrace trace_(h, "adv_l2_error", (cudaStream_t)stream);
   if (!h || !u || !out)
     return fail(ADV_ERR_INVALID, "null argument");
   if (int e = check_device(h))

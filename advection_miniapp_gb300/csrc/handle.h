@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "../../include/advection_gb300.h"
 #include "geometry.h"
@@ -35,6 +37,13 @@ struct adv_handle
   // per cell (v0, v1, v2, 1/|K|): cell average of J^{-1} a and inverse volume, for the FDM preconditioner
   double *d_fdm_cell_d = nullptr;
   float  *d_fdm_cell_f = nullptr;
+  // call timing (adv_set_timing): event pairs around the device work of each
+  // timed call, folded into the totals when queried
+  bool                                            timing = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timed_events;
+  double                                          timed_seconds = 0.0;
+  int64_t                                         timed_calls   = 0;
+  int                                             trace_depth   = 0; // entry points nested in a traced call
 };
 
 
@@ -53,6 +62,22 @@ int            check_device(const adv_handle *h);
 int            ensure_tables(int device);
 // arguments of the projection / mass-energy / L2-error kernels for a mesh
 void           make_diag(const adv_config &cfg, const adv::Mesh &m, const adv::Tables1D &tb, adv::DiagArgs &g);
+// An NVTX range named after the entry point for the duration of the call
+// and, when the handle times its calls, a pair of events around the device
+// work the call enqueues on its stream.
+class CallTrace
+{
+public:
+  CallTrace(adv_handle *h, const char *name, cudaStream_t s);
+  ~CallTrace();
+  CallTrace(const CallTrace &)            = delete;
+  CallTrace &operator=(const CallTrace &) = delete;
+
+private:
+  adv_handle  *h_  = nullptr;
+  cudaStream_t s_  = nullptr;
+  cudaEvent_t  e0_ = nullptr;
+};
 } // namespace detail
 } // namespace adv
 

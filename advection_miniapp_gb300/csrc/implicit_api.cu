@@ -87,6 +87,7 @@ extern "C" {
 
 int adv_vmult(adv_handle *h, const double *src, double *dst, double mass_factor, double t, void *stream)
 {
+  adv::detail::CallTrace trace_(h, "adv_vmult", (cudaStream_t)stream);
   if (!h || !src || !dst)
     return fail(ADV_ERR_INVALID, "null argument");
   if (src == dst)
@@ -215,6 +216,7 @@ int adv_solver_device_bytes(const adv_solver *S, int64_t *out)
 
 int adv_precondition(adv_solver *S, const double *src, double *dst, double mass_factor, double t, void *stream)
 {
+  adv::detail::CallTrace trace_(S ? S->h : nullptr, "adv_precondition", (cudaStream_t)stream);
   if (!S || !src || !dst)
     return fail(ADV_ERR_INVALID, "null argument");
   if (src == dst)
@@ -238,6 +240,7 @@ int adv_precondition(adv_solver *S, const double *src, double *dst, double mass_
 int adv_fgmres(adv_solver *S, double mass_factor, double t, const double *rhs, double *x, double rel_tol,
                int max_iterations, int *iterations, double *rel_residual, void *stream)
 {
+  adv::detail::CallTrace trace_(S ? S->h : nullptr, "adv_fgmres", (cudaStream_t)stream);
   if (!S || !rhs || !x)
     return fail(ADV_ERR_INVALID, "null argument");
   if (rhs == x)
@@ -354,6 +357,7 @@ int adv_fgmres(adv_solver *S, double mass_factor, double t, const double *rhs, d
 int adv_bdf2_step(adv_solver *S, double t_new, double dt, int first_step, const double *u_n, const double *u_nm1,
                   double *u_new, double rel_tol, int *iterations, void *stream)
 {
+  adv::detail::CallTrace trace_(S ? S->h : nullptr, "adv_bdf2_step", (cudaStream_t)stream);
   if (!S || !u_n || !u_new || (!first_step && !u_nm1))
     return fail(ADV_ERR_INVALID, "null argument");
   if (u_new == u_n || u_new == u_nm1)

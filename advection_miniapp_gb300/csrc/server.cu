@@ -49,7 +49,8 @@ struct SReq
   int                 steps = 0, steps_done = 0;
   double             *u = nullptr, *r = nullptr, *k = nullptr;
   double             *t0 = nullptr, *t1 = nullptr; // face traces (collocation groups)
-  int                 state = 0; // 0 queued, 1 active, 2 done, 3 failed (device memory or launch at admission)
+  int                 state = 0; // 0 queued, 1 active, 2 done, 3 failed (device memory or launch at admission), 4 cancelled
+  bool                cancel = false; // cancellation requested while active
   double              t_submit = 0, t_admit = 0, t_done = 0, rel_l2 = -1;
   std::vector<double> solution;
   adv::DiagArgs       diag;
@@ -226,6 +227,23 @@ int rebuild(adv_server *S, SGroup &g)
   ADV_CUDA(cudaMemcpyAsync(g.d_counts, counts, sizeof(counts), cudaMemcpyHostToDevice, g.stream));
   // pageable sources: the copies above are staged before they return
   g.dirty = false;
+  return ADV_OK;
+}
+
+// an active solve leaves without a result (cancelled): its memory goes back
+int drop(adv_server *S, SGroup &g, int64_t id)
+{
+  SReq &q = S->reqs[id];
+  for (double *p : {q.u, q.r, q.k, q.t0, q.t1})
+    if (p)
+      ADV_CUDA(cudaFreeAsync(p, g.stream));
+  q.u = q.r = q.k = q.t0 = q.t1 = nullptr;
+  q.state  = 4;
+  q.t_done = now_s();
+  S->used -= q.bytes;
+  --S->active;
+  ++S->completed;
+  g.dirty = true;
   return ADV_OK;
 }
 
@@ -469,7 +487,13 @@ int adv_server_poll(adv_server *S, int *n_completed)
             }
           SReq &r      = S->reqs[g.members[i]];
           r.steps_done = g.h_slots[i].steps_done;
-          if (r.steps_done >= r.steps)
+          if (r.cancel)
+            {
+              if (int e = drop(S, g, g.members[i]))
+                return e;
+              ++done;
+            }
+          else if (r.steps_done >= r.steps)
             {
               if (int e = retire(S, g, g.members[i]))
                 return e;
@@ -520,6 +544,32 @@ int adv_server_poll(adv_server *S, int *n_completed)
   if (n_completed)
     *n_completed = done;
   return ADV_OK;
+}
+
+int adv_server_cancel(adv_server *S, int64_t id)
+{
+  if (!S || id < 0 || id >= (int64_t)S->reqs.size())
+    return fail(ADV_ERR_INVALID, "unknown request");
+  SReq &q = S->reqs[id];
+  if (q.state == 0)
+    {
+      for (auto it = S->queue.begin(); it != S->queue.end(); ++it)
+        if (*it == id)
+          {
+            S->queue.erase(it);
+            break;
+          }
+      q.state  = 4;
+      q.t_done = now_s();
+      ++S->completed;
+      return ADV_OK;
+    }
+  if (q.state == 1)
+    {
+      q.cancel = true; // leaves at the end of its group's current tick
+      return ADV_OK;
+    }
+  return fail(ADV_ERR_INVALID, "request already finished");
 }
 
 int adv_server_drain(adv_server *S)

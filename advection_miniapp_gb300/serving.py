@@ -29,7 +29,7 @@ from ._lib import IC_SINE_GAUSS, MESH_CARTESIAN, PRECISION_FP32_OPERATOR, PRECIS
 
 SIZES = (4, 6, 8, 12, 16, 24, 32)
 DEGREES = (2, 3, 4, 5, 6)
-STATE_QUEUED, STATE_RUNNING, STATE_DONE, STATE_FAILED = 0, 1, 2, 3
+STATE_QUEUED, STATE_RUNNING, STATE_DONE, STATE_FAILED, STATE_CANCELLED = 0, 1, 2, 3, 4
 POLICIES = {"fifo": 0, "shortest": 1}
 
 
@@ -143,6 +143,10 @@ class Server:
         n = ctypes.c_int()
         _lib.check(self._lib.adv_server_poll(self._s, ctypes.byref(n)), "adv_server_poll")
         return n.value
+
+    def cancel(self, rid):
+        """Queued: leaves at once; running: at the end of its group's tick."""
+        _lib.check(self._lib.adv_server_cancel(self._s, rid), "adv_server_cancel")
 
     def drain(self):
         _lib.check(self._lib.adv_server_drain(self._s), "adv_server_drain")

@@ -221,6 +221,17 @@ int adv_fgmres(adv_solver *s, double mass_factor, double t, const double *rhs, d
 int adv_bdf2_step(adv_solver *s, double t_new, double dt, int first_step, const double *u_n, const double *u_nm1,
                   double *u_new, double rel_tol, int *iterations, void *stream);
 
+/* ------------------------------------------------------------------ timing
+ * The reference accumulates the wall time of its operator calls in
+ * computing_times and prints it at destruction (advection_solver.cc:349-372,
+ * 670-690, 708-755).  With timing on, each (outermost) call of adv_apply,
+ * adv_perform_stage, adv_lsrk_steps, the diagnostics and the implicit entry
+ * points records CUDA events around the work it enqueues; adv_timing waits
+ * for them and returns the accumulated device time and the number of timed
+ * calls.  Every entry point also opens an NVTX range named after itself. */
+int adv_set_timing(adv_handle *h, int enable);
+int adv_timing(adv_handle *h, double *seconds, int64_t *calls);
+
 /* ------------------------------------------------------------------ output
  * output_results (advection_solver.cc:1220-1241): a VTU file with the
  * support points of every (owned) cell, k^3 hexahedra per cell and the point
@@ -260,11 +271,15 @@ int adv_server_submit(adv_server *s, const adv_config *cfg, double t_end, double
  * (relative L2 error against the exact solution), admit queued ones, start the
  * next tick of idle groups.  *n_completed: solves retired in this round. */
 int adv_server_poll(adv_server *s, int *n_completed);
+/* Cancels a request: a queued one leaves the queue at once, a running one at
+ * the end of its group's current tick (its memory then goes back); state 4. */
+int adv_server_cancel(adv_server *s, int64_t request_id);
 /* Polls until every submitted request is complete. */
 int adv_server_drain(adv_server *s);
 /* state: 0 queued, 1 running, 2 done, 3 failed at admission (its device
  * memory could not be allocated or its set-up launch failed; the server
- * carries on with the other requests); latency from submission to retirement. */
+ * carries on with the other requests), 4 cancelled; latency from submission
+ * to retirement. */
 int adv_server_result(adv_server *s, int64_t request_id, int *state, double *rel_l2_error, double *latency_s,
                       int *steps, double *dt);
 /* Final solution of a done request (servers created with keep_solutions != 0). */

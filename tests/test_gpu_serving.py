@@ -130,3 +130,50 @@ def test_shortest_first_policy_same_results(cuda, adv_lib):
     work = {r.index: r.work() for r in reqs}
     small, big = min(work, key=work.get), max(work, key=work.get)
     assert res_s[small]["latency_s"] < res_s[big]["latency_s"]
+
+
+def test_cancel_queued_and_running_requests(cuda, adv_lib):
+    """Cancelling frees the request's memory and lets the others finish with
+    the results they have alone."""
+    from advection_miniapp_gb300.serving import (STATE_CANCELLED, STATE_DONE, STATE_RUNNING, Request, Server)
+    long_run = Request(0, 4, 3, (1.0, 0.0, 0.0), (0.0, 0.0, 0.0), 5.0, 0)   # about 700 steps
+    short = Request(1, 3, 2, (0.0, 1.0, 0.0), (0.0, 0.0, 0.0), 0.05, 1)
+    with Server(keep_solutions=True, max_active=1, steps_per_tick=2) as srv:
+        a = srv.submit(long_run)
+        b = srv.submit(short)
+        c = srv.submit(short)
+        srv.poll()                                   # admits a only (max_active 1)
+        assert srv.result(a)["state"] == STATE_RUNNING
+        srv.cancel(b)                                # queued: leaves at once
+        assert srv.result(b)["state"] == STATE_CANCELLED
+        srv.cancel(a)                                # running: leaves after its tick
+        srv.drain()
+        assert srv.result(a)["state"] == STATE_CANCELLED
+        assert srv.result(c)["state"] == STATE_DONE
+        st = srv.stats()
+        assert st["device_bytes"] == 0 and st["completed"] == 3 and st["running"] == 0
+        with pytest.raises(adv_lib.AdvError):
+            srv.cancel(c)
+        sol = srv.solution(c, short.n_dofs)
+    with Server(keep_solutions=True) as srv:
+        rid = srv.submit(short)
+        srv.drain()
+        np.testing.assert_array_equal(srv.solution(rid, short.n_dofs), sol)
+
+
+def test_call_timing(cuda, adv_lib):
+    """adv_set_timing / adv_timing: the device time of the timed calls
+    (outermost only), like the reference's computing_times."""
+    op = adv_lib.AdvectionOperation(degree=3, n_cells=(6, 6, 6), mesh_type=1, deformation=0.05)
+    u, r, k = (op.initialize_dof_vector() for _ in range(3))
+    op.project_initial(u)
+    assert op.timing() == (0.0, 0)
+    op.set_timing(True)
+    op.lsrk_steps(adv_lib.LSRK_5_4, 0.0, 1e-3, 4, u, r, k)
+    d = op.initialize_dof_vector()
+    op.apply(u, d, 0.0)
+    sec, calls = op.timing()
+    assert calls == 2 and sec > 0.0
+    op.set_timing(False)
+    op.apply(u, d, 0.0)
+    assert op.timing()[1] == 2
