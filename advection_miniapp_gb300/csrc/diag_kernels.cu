@@ -52,6 +52,30 @@ __device__ void tsweep(const double *A, int mo, int ni, int d, int d0, int d1, i
   __syncthreads();
 }
 
+// K sweeps with the same shape at once (one barrier): outs[k] = As[k]
+// applied along d of ins[k]
+template <int K>
+__device__ void tsweep_n(const double *const (&As)[K], const double *const (&ins)[K], double *const (&outs)[K],
+                         int mo, int ni, int d, int d0, int d1, int d2)
+{
+  const int o0 = d == 0 ? mo : d0, o1 = d == 1 ? mo : d1, o2 = d == 2 ? mo : d2;
+  const int total = o0 * o1 * o2;
+  const int st    = d == 0 ? 1 : d == 1 ? d0 : d0 * d1;
+  for (int idx = threadIdx.x; idx < K * total; idx += blockDim.x)
+    {
+      const int kk = idx / total, r = idx % total;
+      const int i0 = r % o0, i1 = (r / o0) % o1, i2 = r / (o0 * o1);
+      const int q  = d == 0 ? i0 : d == 1 ? i1 : i2;
+      const int b  = (d == 0 ? 0 : i0) + d0 * ((d == 1 ? 0 : i1) + d1 * (d == 2 ? 0 : i2));
+      const double *A = As[kk], *in = ins[kk];
+      double        s = 0.0;
+      for (int k = 0; k < ni; ++k)
+        s = fma(A[q * ni + k], in[b + k * st], s);
+      outs[kk][r] = s;
+    }
+  __syncthreads();
+}
+
 // support points of a curved cell, the three components X[c * n^3 + i]; each
 // sine of the deformation depends on one coordinate, so the 3n values
 // sin(2 pi s_d) at the nodes along each direction (sn) serve all n^3 points
@@ -96,15 +120,11 @@ __device__ void map_points(const DiagArgs &g, int m, const double *V, const doub
   for (int c = 0; c < 3; ++c)
     {
       const double *X = s.X + c * nq;
-      tsweep(V, m, n, 2, n, n, n, X, s.A);
-      tsweep(W, m, n, 2, n, n, n, X, s.Az);
-      tsweep(V, m, n, 1, n, n, m, s.A, s.B);
-      tsweep(W, m, n, 1, n, n, m, s.A, s.By);
-      tsweep(V, m, n, 1, n, n, m, s.Az, s.Bz);
-      tsweep(V, m, n, 0, n, m, m, s.B, x + c * m3);
-      tsweep(W, m, n, 0, n, m, m, s.B, J + (3 * c + 0) * m3);
-      tsweep(V, m, n, 0, n, m, m, s.By, J + (3 * c + 1) * m3);
-      tsweep(V, m, n, 0, n, m, m, s.Bz, J + (3 * c + 2) * m3);
+      tsweep_n<2>({V, W}, {X, X}, {s.A, s.Az}, m, n, 2, n, n, n);
+      tsweep_n<3>({V, W, V}, {s.A, s.A, s.Az}, {s.B, s.By, s.Bz}, m, n, 1, n, n, m);
+      tsweep_n<4>({V, W, V, V}, {s.B, s.B, s.By, s.Bz},
+                  {x + c * m3, J + (3 * c + 0) * m3, J + (3 * c + 1) * m3, J + (3 * c + 2) * m3}, m, n, 0, n, m,
+                  m);
     }
 }
 
@@ -176,36 +196,44 @@ __device__ void block_reduce3(double v0, double v1, double v2, double *out)
     }
 }
 
-// shared-memory layout (doubles): X[3], A, Az, B, By, Bz, x[3], J[9], U, T1, T2, T3, sn
-constexpr int kSmemDoubles = 3 * kMaxN3 + 2 * kMaxP * kMaxP * 7 + 3 * kMaxP * kMaxP * 7 + 12 * kMaxP3 + kMaxN3 +
-                             3 * kMaxP3 + 3 * kMaxP;
+// shared-memory layout (doubles) for n points per direction and P = n + 1
+// (the most points of any rule used): X[3][n^3], A, Az [n n P], B, By, Bz
+// [n P P], x[3][P^3], J[9][P^3], U[n^3], T1, T2, T3 [P^3], sn[3n]
+__host__ __device__ inline int diag_smem_doubles(int n)
+{
+  const int P = n + 1, P3 = P * P * P, N3 = n * n * n;
+  return 3 * N3 + 2 * n * n * P + 3 * n * P * P + 12 * P3 + N3 + 3 * P3 + 3 * n;
+}
+constexpr int kSmemDoubles = 3 * kMaxN3 + 2 * 7 * 7 * kMaxP + 3 * 7 * kMaxP * kMaxP + 12 * kMaxP3 + kMaxN3 +
+                             3 * kMaxP3 + 3 * 7;
 
 struct Layout
 {
   Scratch s;
   double *x, *J, *U, *T1, *T2, *T3;
-  __device__ explicit Layout(double *base)
+  __device__ Layout(double *base, int n)
   {
+    const int P = n + 1, P3 = P * P * P, N3 = n * n * n;
     s.X  = base;
-    s.A  = s.X + 3 * kMaxN3;
-    s.Az = s.A + kMaxP * kMaxP * 7;
-    s.B  = s.Az + kMaxP * kMaxP * 7;
-    s.By = s.B + kMaxP * kMaxP * 7;
-    s.Bz = s.By + kMaxP * kMaxP * 7;
-    x    = s.Bz + kMaxP * kMaxP * 7;
-    J    = x + 3 * kMaxP3;
-    U    = J + 9 * kMaxP3;
-    T1   = U + kMaxN3;
-    T2   = T1 + kMaxP3;
-    T3   = T2 + kMaxP3;
-    s.sn = T3 + kMaxP3;
+    s.A  = s.X + 3 * N3;
+    s.Az = s.A + n * n * P;
+    s.B  = s.Az + n * n * P;
+    s.By = s.B + n * P * P;
+    s.Bz = s.By + n * P * P;
+    x    = s.Bz + n * P * P;
+    J    = x + 3 * P3;
+    U    = J + 9 * P3;
+    T1   = U + N3;
+    T2   = T1 + P3;
+    T3   = T2 + P3;
+    s.sn = T3 + P3;
   }
 };
 
 __global__ void __launch_bounds__(kDiagThreads) project_kernel(const DiagArgs g, double t, double *dst)
 {
   extern __shared__ __align__(16) double smem[];
-  Layout    L(smem);
+  Layout    L(smem, g.n);
   const int n = g.n, nq = n * n * n;
   for (long long c = g.cell_begin + blockIdx.x; c < g.n_cells; c += gridDim.x)
     {
@@ -237,7 +265,7 @@ __global__ void __launch_bounds__(kDiagThreads)
   mass_energy_kernel(const DiagArgs g, const double *u, double *partials)
 {
   extern __shared__ __align__(16) double smem[];
-  Layout    L(smem);
+  Layout    L(smem, g.n);
   const int n = g.n, nq = n * n * n;
   double    m = 0.0, e = 0.0, hs = 0.0;
   double   *G[3] = {L.s.A, L.s.B, L.s.By}; // reuse scratch for the three gradients
@@ -285,7 +313,7 @@ __global__ void __launch_bounds__(kDiagThreads)
   l2_error_kernel(const DiagArgs g, const double *u, double t, double *partials)
 {
   extern __shared__ __align__(16) double smem[];
-  Layout    L(smem);
+  Layout    L(smem, g.n);
   const int n = g.n, nq = n * n * n, m = n + 1, m3 = m * m * m;
   double    err = 0.0, nrm = 0.0;
   for (long long c = g.cell_begin + blockIdx.x; c < g.n_cells; c += gridDim.x)
@@ -382,7 +410,8 @@ cudaError_t launch_project(const DiagArgs &g, double t, double *dst, cudaStream_
 {
   if (cudaError_t e = opt_in(project_kernel))
     return e;
-  project_kernel<<<diag_max_blocks(g.n_cells - g.cell_begin), kDiagThreads, kSmemBytes, s>>>(g, t, dst);
+  project_kernel<<<diag_max_blocks(g.n_cells - g.cell_begin), kDiagThreads,
+                   diag_smem_doubles(g.n) * sizeof(double), s>>>(g, t, dst);
   return cudaGetLastError();
 }
 
@@ -392,7 +421,7 @@ cudaError_t launch_mass_energy(const DiagArgs &g, const double *u, double *parti
   if (cudaError_t e = opt_in(mass_energy_kernel))
     return e;
   *n_blocks = diag_max_blocks(g.n_cells - g.cell_begin);
-  mass_energy_kernel<<<*n_blocks, kDiagThreads, kSmemBytes, s>>>(g, u, partials);
+  mass_energy_kernel<<<*n_blocks, kDiagThreads, diag_smem_doubles(g.n) * sizeof(double), s>>>(g, u, partials);
   return cudaGetLastError();
 }
 
@@ -402,7 +431,7 @@ cudaError_t launch_l2_error(const DiagArgs &g, const double *u, double t, double
   if (cudaError_t e = opt_in(l2_error_kernel))
     return e;
   *n_blocks = diag_max_blocks(g.n_cells - g.cell_begin);
-  l2_error_kernel<<<*n_blocks, kDiagThreads, kSmemBytes, s>>>(g, u, t, partials);
+  l2_error_kernel<<<*n_blocks, kDiagThreads, diag_smem_doubles(g.n) * sizeof(double), s>>>(g, u, t, partials);
   return cudaGetLastError();
 }
 
