@@ -186,11 +186,12 @@ int validate(const adv_config &c)
       if (!(c.domain_hi[d] > c.domain_lo[d]))
         return fail(ADV_ERR_INVALID, "domain_hi must exceed domain_lo");
     }
+  // vector indices are 64-bit everywhere (cell offset x points per cell),
+  // cell indices are 32-bit: the cell count is the limit, device memory the
+  // practical one
   const double nc = (double)c.n_cells[0] * c.n_cells[1] * c.n_cells[2];
-  if (nc * std::pow(c.degree + 1.0, 3) > 2.0e9)
-    return fail(ADV_ERR_INVALID, "more than 2e9 degrees of freedom are not supported");
   if (nc > 2.0e9)
-    return fail(ADV_ERR_INVALID, "too many cells");
+    return fail(ADV_ERR_INVALID, "more than 2e9 cells are not supported");
   if (c.mesh_type != ADV_MESH_CARTESIAN && c.mesh_type != ADV_MESH_DEFORMED)
     return fail(ADV_ERR_INVALID, "unknown mesh_type");
   if (c.mesh_type == ADV_MESH_DEFORMED && !(std::fabs(c.deformation) < 0.1))
