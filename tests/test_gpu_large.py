@@ -1,5 +1,5 @@
-"""Maximum sizes: a mesh with more than 2^31 DoFs (256^3 affine periodic
-cells of degree 4, 2,147,483,648 DoFs; about 90 GB of device memory with the
+"""Maximum sizes: a mesh with more than 2^31 DoFs (272^3 affine periodic
+cells of degree 4, 2,515,456,000 DoFs; about 110 GB of device memory with the
 step loop's face traces).  Every index into the vectors, the traces and the
 face data must be 64-bit: an overflow anywhere shows as an O(1) error."""
 import numpy as np
@@ -11,10 +11,10 @@ pytestmark = pytest.mark.gpu
 def test_more_than_2_31_dofs(cuda, adv_lib):
     torch = cuda
     free, total = torch.cuda.mem_get_info()
-    if free < 120 * 2 ** 30:
-        pytest.skip("needs about 100 GB of free device memory")
-    op = adv_lib.AdvectionOperation(degree=4, n_cells=(256, 256, 256), velocity=(1.0, 0.15, -0.05))
-    assert op.n_dofs == 256 ** 3 * 125 > 2 ** 31
+    if free < 130 * 2 ** 30:
+        pytest.skip("needs about 110 GB of free device memory")
+    op = adv_lib.AdvectionOperation(degree=4, n_cells=(272, 272, 272), velocity=(1.0, 0.15, -0.05))
+    assert op.n_dofs == 272 ** 3 * 125 > 2 ** 31
     u = op.initialize_dof_vector()
     op.project_initial(u)
     e0, n0 = op.l2_error(u, 0.0)
@@ -24,7 +24,7 @@ def test_more_than_2_31_dofs(cuda, adv_lib):
     op.lsrk_steps(adv_lib.LSRK_5_4, 0.0, dt, 2, u, r, k)
     e, nrm = op.l2_error(u, 2 * dt)
     m = op.compute_mass_and_energy(u)
-    # degree 4 at h = 1/256: the projection error is about 1e-11 and two steps add little
+    # degree 4 at h = 1/272: the projection error is about 1e-11 and two steps add little
     assert e / nrm < 10 * e0 / n0 + 1e-10, (e / nrm, e0 / n0)
     assert abs(m[0] - m0[0]) <= 1e-12 * abs(m0[1]) ** 0.5
     # the cells at the two ends of the vector (beyond 2^31 values) agree with the exact solution too
