@@ -24,11 +24,12 @@ def test_more_than_2_31_dofs(cuda, adv_lib):
     op.lsrk_steps(adv_lib.LSRK_5_4, 0.0, dt, 2, u, r, k)
     e, nrm = op.l2_error(u, 2 * dt)
     m = op.compute_mass_and_energy(u)
-    # degree 4 at h = 1/272: the projection error is about 1e-11 and two steps add little
-    assert e / nrm < 10 * e0 / n0 + 1e-10, (e / nrm, e0 / n0)
+    # the projection error is 1.3e-12; the steps add about 6e-7 per unit time
+    # at any resolution (the Gaussian part of the data is not periodic: its
+    # derivative jumps by 4e-4 across the domain boundary), 3e-10 here; an
+    # index overflow anywhere would show as an O(1) error
+    assert e0 / n0 < 1e-11 and e / nrm < 1e-9, (e / nrm, e0 / n0)
     assert abs(m[0] - m0[0]) <= 1e-12 * abs(m0[1]) ** 0.5
-    # the cells at the two ends of the vector (beyond 2^31 values) agree with the exact solution too
-    tail = u[-125 * 4096:].clone()
-    assert torch.isfinite(tail).all()
+    assert torch.isfinite(u[-125 * 4096:]).all()
     del u, r, k
     torch.cuda.empty_cache()
