@@ -50,6 +50,11 @@ struct StageShape
   static constexpr int VALUES =
     2 * C * NQ + 6 * C * NF + (UNI ? 0 : 4 * C * NQ + 12 * C * NF) + (VISC ? 6 * C * NF : 0);
   static constexpr int SMEM   = VALUES * (int)sizeof(T) + 12 * C * (int)sizeof(int);
+  // the nodal kernel with the binary32 operator on field geometry reads the
+  // face coefficients from global memory instead of staging them: one more
+  // resident CTA per SM for a latency-bound kernel
+  static constexpr bool FACES_GLOBAL = sizeof(T) == sizeof(float) && !UNI && !VISC;
+  static constexpr int  SMEM_NODAL   = SMEM - (FACES_GLOBAL ? 12 * C * NF * (int)sizeof(T) : 0);
   // the cell geometry Gb (after Ub, Qb, Nb) is filled by 16-byte cp.async
   static_assert((2 * C * NQ + 6 * C * NF) * (int)sizeof(T) % 16 == 0, "cp.async destinations need 16-byte alignment");
 };
@@ -496,8 +501,9 @@ __device__ __forceinline__ void stage_cta(const StageArgs &A, const long long ce
   T   *Qb     = Ub + C * NQ;                     // [C][NQ] accumulated Z, then k
   T   *Nb     = Qb + C * NQ;                     // [C][6][NF] neighbour face values
   T   *Gb     = Nb + C * 6 * NF;                 // field: [C][4][NQ] cell geometry
-  T   *Fb     = Gb + (UNI ? 0 : C * 4 * NQ);     // field: [C][6][2][NF] face coefficients
-  T   *Nd     = Fb + (UNI ? 0 : C * 12 * NF);    // viscous: [C][6][NF] neighbour normal derivatives
+  constexpr bool FG = SH::FACES_GLOBAL;
+  T   *Fb     = Gb + (UNI ? 0 : C * 4 * NQ);     // field: [C][6][2][NF] face coefficients (staged unless FG)
+  T   *Nd     = Fb + (UNI || FG ? 0 : C * 12 * NF); // viscous: [C][6][NF] neighbour normal derivatives
   int *s_nbr  = reinterpret_cast<int *>(Nd + (VISC ? C * 6 * NF : 0)); // [C][6] neighbour or -1
   int *s_face = s_nbr + C * 6;                                          // [C][6] face id
 
@@ -521,7 +527,17 @@ __device__ __forceinline__ void stage_cta(const StageArgs &A, const long long ce
   // ---- phase 0b: curved meshes / variable velocity: start the asynchronous
   //      copies of the geometry; they land while the sweeps below run
   if (!UNI)
-    geometry_async<N, T>(A, cell0, ncell, s_face, Gb, Fb, tid, NT);
+    geometry_async<N, T>(A, cell0, ncell, s_face, Gb, Fb, tid, NT, !FG);
+  // face coefficients [P | M] of face j of local cell cl: staged or global
+  auto faces = [&](int cl, int j) -> const T * {
+    if (FG)
+      {
+        const int d = j >> 1;
+        const T  *F = static_cast<const T *>(d == 0 ? A.face_geo[0] : d == 1 ? A.face_geo[1] : A.face_geo[2]);
+        return F + (size_t)s_face[cl * 6 + j] * 2 * NF;
+      }
+    return Fb + (cl * 6 + j) * 2 * NF;
+  };
 
   // ---- phase 1: own values loaded as z-pencils and interpolated along z;
   //      neighbour face layers loaded as rows along their first tangential
@@ -672,12 +688,12 @@ __device__ __forceinline__ void stage_cta(const StageArgs &A, const long long ce
 #pragma unroll
       for (int k = 0; k < N; ++k)
         p[k] = U[k];
-      const T *F = Fb + cl * 12 * NF;
+      const T *F = faces(cl, 0), *Fh = faces(cl, 1);
       direction_pass<N, T, UNI, VISC, 0>(A, tb, U, Nb[(cl * 6 + 0) * NF + r], Nb[(cl * 6 + 1) * NF + r],
                                          VISC ? Nd[(cl * 6 + 0) * NF + r] : T(0),
                                          VISC ? Nd[(cl * 6 + 1) * NF + r] : T(0),
                                          s_nbr[cl * 6 + 0] < 0, s_nbr[cl * 6 + 1] < 0, r,
-                                   F, F + 2 * NF, Gb + cl * 4 * NQ + N * r, 1, out);
+                                   F, Fh, Gb + cl * 4 * NQ + N * r, 1, out);
       T *z = Qb + cl * NQ + N * r;
 #pragma unroll
       for (int k = 0; k < N; ++k)
@@ -695,12 +711,12 @@ __device__ __forceinline__ void stage_cta(const StageArgs &A, const long long ce
 #pragma unroll
       for (int k = 0; k < N; ++k)
         U[k] = p[k * N];
-      const T *F = Fb + cl * 12 * NF + 4 * NF;
+      const T *F = faces(cl, 2), *Fh = faces(cl, 3);
       direction_pass<N, T, UNI, VISC, 1>(A, tb, U, Nb[(cl * 6 + 2) * NF + r], Nb[(cl * 6 + 3) * NF + r],
                                          VISC ? Nd[(cl * 6 + 2) * NF + r] : T(0),
                                          VISC ? Nd[(cl * 6 + 3) * NF + r] : T(0),
                                          s_nbr[cl * 6 + 2] < 0, s_nbr[cl * 6 + 3] < 0, r,
-                                   F, F + 2 * NF, Gb + (cl * 4 + 1) * NQ + off, N, out);
+                                   F, Fh, Gb + (cl * 4 + 1) * NQ + off, N, out);
       T *z = Qb + cl * NQ + off;
 #pragma unroll
       for (int k = 0; k < N; ++k)
@@ -717,13 +733,13 @@ __device__ __forceinline__ void stage_cta(const StageArgs &A, const long long ce
 #pragma unroll
       for (int k = 0; k < N; ++k)
         U[k] = p[k * NF];
-      const T *F = Fb + cl * 12 * NF + 8 * NF;
+      const T *F = faces(cl, 4), *Fh = faces(cl, 5);
       const T *G = Gb + cl * 4 * NQ;
       direction_pass<N, T, UNI, VISC, 2>(A, tb, U, Nb[(cl * 6 + 4) * NF + r], Nb[(cl * 6 + 5) * NF + r],
                                          VISC ? Nd[(cl * 6 + 4) * NF + r] : T(0),
                                          VISC ? Nd[(cl * 6 + 5) * NF + r] : T(0),
                                          s_nbr[cl * 6 + 4] < 0, s_nbr[cl * 6 + 5] < 0, r,
-                                   F, F + 2 * NF, G + 2 * NQ + r, NF, out);
+                                   F, Fh, G + 2 * NQ + r, NF, out);
       T *z = Qb + cl * NQ + r;
       if (A.mode != kModeVmult)
         {
@@ -865,7 +881,7 @@ cudaError_t launch_stage_t(const StageArgs &args, cudaStream_t stream)
         configured |= 1ull << dev;
     }
   const long long blocks = (args.n_cells - args.cell_begin + SH::C - 1) / SH::C;
-  stage_kernel<N, T, UNI, VISC><<<(unsigned)blocks, SH::THREADS, SH::SMEM, stream>>>(args);
+  stage_kernel<N, T, UNI, VISC><<<(unsigned)blocks, SH::THREADS, SH::SMEM_NODAL, stream>>>(args);
   return cudaGetLastError();
 }
 
