@@ -56,7 +56,7 @@ struct GaussShape
   // kernels lose 7 % (FP64) and 4 % (FP32) with global geometry, so they keep
   // staging it.
   static constexpr bool GEO_GLOBAL   = VISC;
-  static constexpr bool FACES_GLOBAL = (TR && !UNI) || VISC;
+  static constexpr bool FACES_GLOBAL = !UNI && (TR || VISC || sizeof(T) == sizeof(float));
   static constexpr int  FB_VALUES    = UNI || FACES_GLOBAL ? 0 : 12 * C * N * N;
   static constexpr int  GB_VALUES    = UNI || GEO_GLOBAL ? 0 : 4 * C * N * N * N;
   static constexpr int  SMEM = SH::SMEM + TB_VALUES * (int)sizeof(T) -
