@@ -248,6 +248,22 @@ class AdvectionOperation:
             self._h, int(scheme), float(time), float(time_step), int(n_steps), self._ptr(solution),
             self._ptr(vec_ri), self._ptr(vec_ki), _stream_handle(stream)), "adv_lsrk_steps")
 
+    def lsrk_steps_host(self, scheme, time, time_step, n_steps, host_solution, solution, vec_ri, vec_ki,
+                        stream=None):
+        """lsrk_steps on a solution in host memory (a contiguous CPU float64
+        tensor, best page-locked): copied into `solution`, advanced and copied
+        back, the copies overlapped with the first and last stages.  The host
+        tensor holds the result once the stream has passed the call."""
+        import torch
+        if not (isinstance(host_solution, torch.Tensor) and not host_solution.is_cuda
+                and host_solution.dtype == torch.float64 and host_solution.is_contiguous()
+                and host_solution.numel() == self.n_dofs):
+            raise ValueError(f"expected a contiguous CPU float64 tensor of {self.n_dofs} entries")
+        _lib.check(self._lib.adv_lsrk_steps_host(
+            self._h, int(scheme), float(time), float(time_step), int(n_steps),
+            ctypes.c_void_p(host_solution.data_ptr()), self._ptr(solution), self._ptr(vec_ri), self._ptr(vec_ki),
+            _stream_handle(stream)), "adv_lsrk_steps_host")
+
 
 class LowStorageRungeKuttaIntegrator:
     """Counterpart of the reference's LowStorageRungeKuttaIntegrator (advection_solver.cc:822-944)."""

@@ -66,6 +66,7 @@ SIGNATURES = {
     "adv_perform_stage": (_I, [_P, _D, _D, _D, _P, _P, _P, _P, _P]),
     "adv_lsrk_step": (_I, [_P, _I, _D, _D, _P, _P, _P, _P]),
     "adv_lsrk_steps": (_I, [_P, _I, _D, _D, _I, _P, _P, _P, _P]),
+    "adv_lsrk_steps_host": (_I, [_P, _I, _D, _D, _I, _P, _P, _P, _P, _P]),
     "adv_lsrk_coefficients": (_I, [_I, _DP, _DP, ctypes.POINTER(_I)]),
     "adv_project": (_I, [_P, _D, _P, _P]),
     "adv_mass_energy": (_I, [_P, _P, _DP, _P]),

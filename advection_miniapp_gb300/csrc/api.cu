@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -687,6 +688,11 @@ int adv_destroy(adv_handle *h)
     }
   cudaFree(h->d_traces[0]);
   cudaFree(h->d_traces[1]);
+  for (cudaEvent_t e : h->pipe_events)
+    cudaEventDestroy(e);
+  for (cudaStream_t cs : h->copy_stream)
+    if (cs)
+      cudaStreamDestroy(cs);
   delete h;
   return ADV_OK;
 }
@@ -845,70 +851,93 @@ int adv_lsrk_coefficients(int scheme, double *a, double *b, int *n_stages)
 // written by the previous stage, write the next r to the other one and
 // update U in place.  No stage writes a buffer that neighbouring cells read,
 // and the solution ends in U without copies.
+extern "C++" {
 namespace
 {
+// stage time of stage st of the step starting at t0 (the reference's
+// accumulation order, advection_solver.cc:916-935)
+double stage_time(const std::vector<double> &ai, const std::vector<double> &bi, double t0, double dt, int st)
+{
+  if (st == 0)
+    return t0;
+  double sum_previous_bi = 0.0;
+  for (int j = 0; j + 1 < st; ++j)
+    sum_previous_bi += bi[j];
+  return t0 + (sum_previous_bi + ai[st - 1]) * dt;
+}
+
+// Stage st of step `step` of the plain step loop.  With face traces, stage g
+// = step * n_stages + st reads the traces of its input from d_traces[g & 1]
+// (the basis change writes those of u into d_traces[0]) and writes those of
+// its output into the other buffer.
+int plain_stage(adv_handle *h, const std::vector<double> &ai, const std::vector<double> &bi, double t, double dt,
+                int step, int st, bool gauss, bool traces, double *u, double *r, double *k, adv::StageArgs &A,
+                int &prec)
+{
+  const int ns = (int)bi.size();
+  A            = base_args(*h, stage_time(ai, bi, t + step * dt, dt, st));
+  prec         = -1;
+  const double fac  = A.out_scale;
+  const bool   last = st == ns - 1;
+  A.gauss           = gauss;
+  if (traces)
+    {
+      const long long g = (long long)step * ns + st;
+      A.tr_in           = h->d_traces[g & 1];
+      A.tr_out          = h->d_traces[(g + 1) & 1];
+    }
+  A.b    = bi[st] * dt * fac;
+  A.a    = last ? 0.0 : ai[st] * dt * fac;
+  A.mode = last ? adv::kModeLastStage : adv::kModeStage;
+  if (st == 0)
+    {
+      A.r_in = u, A.u_in = u, A.u_out = k, A.r_out = r;
+    }
+  else if (st == 1)
+    {
+      A.r_in = r, A.u_in = k, A.u_out = u, A.r_out = k;
+    }
+  else
+    {
+      double *rin  = (st % 2 == 0) ? k : r;
+      double *rout = (st % 2 == 0) ? r : k;
+      A.r_in = rin, A.u_in = u, A.u_out = u, A.r_out = last ? nullptr : rout;
+    }
+  return ADV_OK;
+}
+
 // FP32 increments (ADV_PRECISION_FP32_INCREMENT): per step, stage 0 with the
 // FP64 operator writes K0 = L(u_n), E = b0 dt K0 and G = a0 dt K0 (the
 // increments u - u_n and r - u_n); stages s >= 1 evaluate k = K0 + L32(G_s)
 // and update E and G in FP64; the last stage writes u_n + E + b dt k into u.
 // Buffers: E = r, G alternates between k and a handle scratch vector, K0 in
 // a second scratch vector.
-int lsrk_increment_steps(adv_handle *h, const std::vector<double> &ai, const std::vector<double> &bi, double t,
-                         double dt, int n_steps, double *u, double *r, double *k, cudaStream_t s)
+int increment_stage(adv_handle *h, const std::vector<double> &ai, const std::vector<double> &bi, double t,
+                    double dt, int step, int st, bool gauss, double *u, double *r, double *k, adv::StageArgs &A,
+                    int &prec)
 {
-  if (int e = ensure_scratch(h, 0))
-    return e;
-  if (int e = ensure_scratch(h, 1))
-    return e;
-  const bool gauss = n_steps > 0 && h->cfg.fused_form != ADV_FORM_NODAL;
-  double    *E = r, *Ga = k, *Gb = h->d_scratch[0], *K0 = h->d_scratch[1];
-  const int  ns = (int)bi.size();
-  if (gauss)
+  const int ns = (int)bi.size();
+  double   *E = r, *Ga = k, *Gb = h->d_scratch[0], *K0 = h->d_scratch[1];
+  prec            = st == 0 ? 0 : 1;
+  A               = base_args(*h, stage_time(ai, bi, t + step * dt, dt, st), prec);
+  const bool last = st == ns - 1;
+  A.gauss         = gauss;
+  A.b             = bi[st] * dt * A.out_scale;
+  A.a             = last ? 0.0 : ai[st] * dt * A.out_scale;
+  A.mode          = last ? adv::kModeLastStage : adv::kModeStage;
+  if (st == 0)
     {
-      ADV_CUDA(adv::launch_basis_change(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, true, s));
-      ++h->launches;
+      A.r_in = u, A.u_in = nullptr, A.u_out = E, A.r_out = Ga, A.k_out = K0;
     }
-  for (int step = 0; step < n_steps; ++step)
+  else
     {
-      const double t0 = t + step * dt;
-      double       sum_previous_bi = 0.0;
-      for (int st = 0; st < ns; ++st)
-        {
-          double ts = t0;
-          if (st > 0)
-            {
-              ts = t0 + (sum_previous_bi + ai[st - 1]) * dt;
-              sum_previous_bi += bi[st - 1];
-            }
-          const int      prec = st == 0 ? 0 : 1;
-          adv::StageArgs A    = base_args(*h, ts, prec);
-          const bool     last = st == ns - 1;
-          A.gauss             = gauss;
-          A.b                 = bi[st] * dt * A.out_scale;
-          A.a                 = last ? 0.0 : ai[st] * dt * A.out_scale;
-          A.mode              = last ? adv::kModeLastStage : adv::kModeStage;
-          if (st == 0)
-            {
-              A.r_in = u, A.u_in = nullptr, A.u_out = E, A.r_out = Ga, A.k_out = K0;
-            }
-          else
-            {
-              A.r_in  = (st % 2) ? Ga : Gb;
-              A.k_add = K0;
-              A.u_in  = E;
-              if (last)
-                A.u_out = u, A.u_base = u;
-              else
-                A.u_out = E, A.r_out = (st % 2) ? Gb : Ga;
-            }
-          if (int e = launch(h, A, s, prec))
-            return e;
-        }
-    }
-  if (gauss)
-    {
-      ADV_CUDA(adv::launch_basis_change(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, false, s));
-      ++h->launches;
+      A.r_in  = (st % 2) ? Ga : Gb;
+      A.k_add = K0;
+      A.u_in  = E;
+      if (last)
+        A.u_out = u, A.u_base = u;
+      else
+        A.u_out = E, A.r_out = (st % 2) ? Gb : Ga;
     }
   return ADV_OK;
 }
@@ -920,12 +949,203 @@ bool increment_form_applies(const adv_handle &h)
   return h.cfg.precision == ADV_PRECISION_FP32_INCREMENT && h.cfg.velocity_type == ADV_VELOCITY_CONSTANT &&
          (h.mesh.periodic || h.cfg.boundary_value != ADV_BOUNDARY_EXACT);
 }
-} // namespace
 
-int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, double *u, double *r,
-                   double *k, void *stream)
+// Copies of a host solution in z-layer chunks (adv_lsrk_steps_host): chunk c
+// holds the layers [z[c], z[c + 1]), a contiguous range of cells.
+struct HostChunks
 {
-  adv::detail::CallTrace trace_(h, "adv_lsrk_steps", (cudaStream_t)stream);
+  std::vector<int> z;
+  int64_t          layer_cells = 0, cell_dofs = 0;
+  int              count() const { return (int)z.size() - 1; }
+  int64_t          cell(int layer) const { return layer * layer_cells; }
+  int64_t          dof(int layer) const { return layer * layer_cells * cell_dofs; }
+};
+
+HostChunks plan_chunks(const adv::Mesh &m)
+{
+  // 8 chunks at most, 2 MB at least.  Measured on GB300 with the 262 MB
+  // solution of 64^3 degree-4 cells (FP64 step 13.6 ms without copies, each
+  // copy 1.24-1.36 ms): 4 chunks 14.46 ms, 8 chunks 14.28 ms, 16 chunks
+  // 14.37 ms, 32 chunks 14.85 ms per step with the copies
+  HostChunks    c;
+  const int     nz    = m.nc[2];
+  c.layer_cells       = (int64_t)m.nc[0] * m.nc[1];
+  c.cell_dofs         = (int64_t)m.n * m.n * m.n;
+  const int64_t bytes = m.n_dofs * (int64_t)sizeof(double);
+  int           k     = (int)std::min<int64_t>(std::min(nz, 8), std::max<int64_t>(1, bytes / (2 << 20)));
+  for (int i = 0; i <= k; ++i)
+    c.z.push_back((int)((int64_t)nz * i / k));
+  return c;
+}
+
+int ensure_copy_pipe(adv_handle *h, size_t n_events)
+{
+  for (cudaStream_t &cs : h->copy_stream)
+    if (!cs)
+      ADV_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  while (h->pipe_events.size() < n_events)
+    {
+      cudaEvent_t e = nullptr;
+      ADV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      h->pipe_events.push_back(e);
+    }
+  return ADV_OK;
+}
+
+// The step loop shared by the plain and the increment forms.  stage(step, st,
+// A, prec) fills the arguments of one whole-mesh stage launch.  With gauss
+// the solution moves to the Gauss-point values before the steps and back
+// afterwards (cell by cell; with traces the first change writes the face
+// traces of u as well).
+//
+// With host != nullptr the solution comes from and goes back to host memory,
+// in z-layer chunks on the handle's copy streams.  Chunk c's copy in is
+// followed on the compute stream by its basis change (collocation form) or,
+// in the nodal form, the first stage of the first step runs chunk by chunk as
+// soon as a chunk and the layers next to it have arrived.  The last stage of
+// the last step runs chunk by chunk, each chunk followed by its basis change
+// back and its copy out.  Every cell gets the same arithmetic as in the
+// whole-mesh launches, so the results are the same bit for bit.
+//
+// In the collocation form the first stage runs on the whole mesh after the
+// copies: measured on GB300 (64^3 degree-4 cells, FP64) a chunked first stage
+// overlapping the copies in was 0.15 ms slower per call (14.43 against 14.28
+// ms; the copies write through the L2 the stage reads its neighbours from),
+// while the basis change alone, cell-local streaming, hides most of the 1.24
+// ms copy.
+template <typename StageFn>
+int run_steps(adv_handle *h, int n_steps, int ns, bool gauss, bool traces, double *u, double *host, cudaStream_t s,
+              StageFn stage)
+{
+  const int64_t cb = h->mesh.cell_begin, ce = h->mesh.cell_end;
+  const int     n  = h->mesh.n;
+  double       *tr_basis = traces ? static_cast<double *>(h->d_traces[0]) : nullptr;
+  HostChunks    ch;
+  int           nch = 0;
+  if (host)
+    {
+      ch  = plan_chunks(h->mesh);
+      nch = ch.count();
+      if (int e = ensure_copy_pipe(h, 2 * (size_t)nch + 2))
+        return e;
+    }
+  cudaEvent_t *ev      = h->pipe_events.data();
+  auto         launch_range = [&](adv::StageArgs A, int prec, int z0, int z1) {
+    A.cell_begin = ch.cell(z0);
+    A.n_cells    = ch.cell(z1);
+    return launch(h, A, s, prec);
+  };
+  if (host)
+    {
+      // copy in: chunk c on copy stream 0 after the work already on s; on a
+      // periodic mesh the top chunk goes first, so that the bottom chunk's
+      // first stage does not wait for the end of the copies
+      const int         nz   = h->mesh.nc[2];
+      const bool        wrap = h->mesh.periodic;
+      std::vector<int>  order;
+      if (wrap && nch > 2)
+        order.push_back(nch - 1);
+      for (int c = 0; (int)order.size() < nch; ++c)
+        order.push_back(c);
+      cudaStream_t in = h->copy_stream[0];
+      ADV_CUDA(cudaEventRecord(ev[0], s));
+      ADV_CUDA(cudaStreamWaitEvent(in, ev[0], 0));
+      for (int c : order)
+        {
+          const int64_t d0 = ch.dof(ch.z[c]), d1 = ch.dof(ch.z[c + 1]);
+          ADV_CUDA(cudaMemcpyAsync(u + d0, host + d0, (d1 - d0) * sizeof(double), cudaMemcpyHostToDevice, in));
+          ADV_CUDA(cudaEventRecord(ev[1 + c], in));
+        }
+      adv::StageArgs A0;
+      int            prec0 = -1;
+      if (n_steps > 0)
+        if (int e = stage(0, 0, A0, prec0))
+          return e;
+      std::vector<char> arrived(nz, 0), staged(nch, 0);
+      auto              ready = [&](int layer) {
+        if (layer < 0 || layer >= nz)
+          return wrap ? arrived[(layer + nz) % nz] != 0 : true;
+        return arrived[layer] != 0;
+      };
+      for (int c : order)
+        {
+          ADV_CUDA(cudaStreamWaitEvent(s, ev[1 + c], 0));
+          if (gauss)
+            {
+              ADV_CUDA(adv::launch_basis_change(n, u, ch.cell(ch.z[c]), ch.cell(ch.z[c + 1]), true, s, tr_basis,
+                                                trace_width(*h)));
+              ++h->launches;
+            }
+          for (int l = ch.z[c]; l < ch.z[c + 1]; ++l)
+            arrived[l] = 1;
+          if (n_steps == 0 || gauss)
+            continue;
+          // first stage of every chunk whose cells and neighbour layers are in
+          for (int j = 0; j < nch; ++j)
+            if (!staged[j] && ready(ch.z[j] - 1) && ready(ch.z[j + 1]))
+              {
+                bool all = true;
+                for (int l = ch.z[j]; l < ch.z[j + 1]; ++l)
+                  all = all && arrived[l];
+                if (!all)
+                  continue;
+                if (int e = launch_range(A0, prec0, ch.z[j], ch.z[j + 1]))
+                  return e;
+                staged[j] = 1;
+              }
+        }
+    }
+  else if (gauss)
+    {
+      ADV_CUDA(adv::launch_basis_change(n, u, cb, ce, true, s, tr_basis, trace_width(*h)));
+      ++h->launches;
+    }
+  for (int step = 0; step < n_steps; ++step)
+    for (int st = 0; st < ns; ++st)
+      {
+        if (host && step == 0 && st == 0 && !gauss)
+          continue; // ran chunk by chunk with the copies in
+        adv::StageArgs A;
+        int            prec = -1;
+        if (int e = stage(step, st, A, prec))
+          return e;
+        if (!(host && step == n_steps - 1 && st == ns - 1))
+          {
+            if (int e = launch(h, A, s, prec))
+              return e;
+            continue;
+          }
+        // last stage with the copies out: chunk c on copy stream 1 after its
+        // stage and basis change
+        cudaStream_t out = h->copy_stream[1];
+        for (int c = 0; c < nch; ++c)
+          {
+            if (int e = launch_range(A, prec, ch.z[c], ch.z[c + 1]))
+              return e;
+            if (gauss)
+              {
+                ADV_CUDA(adv::launch_basis_change(n, u, ch.cell(ch.z[c]), ch.cell(ch.z[c + 1]), false, s));
+                ++h->launches;
+              }
+            const int64_t d0 = ch.dof(ch.z[c]), d1 = ch.dof(ch.z[c + 1]);
+            ADV_CUDA(cudaEventRecord(ev[1 + nch + c], s));
+            ADV_CUDA(cudaStreamWaitEvent(out, ev[1 + nch + c], 0));
+            ADV_CUDA(cudaMemcpyAsync(host + d0, u + d0, (d1 - d0) * sizeof(double), cudaMemcpyDeviceToHost, out));
+          }
+        ADV_CUDA(cudaEventRecord(ev[1 + 2 * nch], out));
+        ADV_CUDA(cudaStreamWaitEvent(s, ev[1 + 2 * nch], 0));
+      }
+  if (gauss && !host)
+    {
+      ADV_CUDA(adv::launch_basis_change(n, u, cb, ce, false, s));
+      ++h->launches;
+    }
+  return ADV_OK;
+}
+
+int lsrk_steps_impl(adv_handle *h, int scheme, double t, double dt, int n_steps, double *u, double *r, double *k,
+                    double *host, cudaStream_t s)
+{
   if (!h || !u || !r || !k)
     return fail(ADV_ERR_INVALID, "null argument");
   if (u == r || u == k || r == k)
@@ -940,12 +1160,26 @@ int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, 
   std::vector<double> ai, bi;
   if (!adv::lsrk_coefficients(scheme, ai, bi))
     return fail(ADV_ERR_INVALID, "unknown LSRK scheme");
-  cudaStream_t s  = (cudaStream_t)stream;
-  const int    ns = (int)bi.size();
+  const int ns = (int)bi.size();
   if (ns == 1)
     return fail(ADV_ERR_INVALID, "one-stage schemes are not supported");
+  if (host && n_steps == 0)
+    {
+      ADV_CUDA(cudaMemcpyAsync(u, host, h->mesh.n_dofs * sizeof(double), cudaMemcpyHostToDevice, s));
+      return ADV_OK;
+    }
   if (increment_form_applies(*h))
-    return lsrk_increment_steps(h, ai, bi, t, dt, n_steps, u, r, k, s);
+    {
+      if (int e = ensure_scratch(h, 0))
+        return e;
+      if (int e = ensure_scratch(h, 1))
+        return e;
+      const bool gauss = n_steps > 0 && h->cfg.fused_form != ADV_FORM_NODAL;
+      return run_steps(h, n_steps, ns, gauss, false, u, host, s,
+                       [&](int step, int st, adv::StageArgs &A, int &prec) {
+                         return increment_stage(h, ai, bi, t, dt, step, st, gauss, u, r, k, A, prec);
+                       });
+    }
   // collocation form: the solution moves to the Gauss-point values for the
   // steps and back afterwards (r and k are scratch either way)
   const bool gauss  = n_steps > 0 && use_collocation(*h);
@@ -953,62 +1187,27 @@ int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, 
   if (traces)
     if (int e = ensure_traces(h))
       return e;
-  void *tr_in = h->d_traces[0], *tr_out = h->d_traces[1];
-  if (gauss)
-    {
-      ADV_CUDA(adv::launch_basis_change(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, true, s,
-                                        traces ? static_cast<double *>(tr_in) : nullptr, trace_width(*h)));
-      ++h->launches;
-    }
-  for (int step = 0; step < n_steps; ++step)
-    {
-      const double t0 = t + step * dt;
-      double       sum_previous_bi = 0.0;
-      for (int st = 0; st < ns; ++st)
-        {
-          double ts = t0;
-          if (st > 0)
-            {
-              ts = t0 + (sum_previous_bi + ai[st - 1]) * dt;
-              sum_previous_bi += bi[st - 1];
-            }
-          adv::StageArgs A   = base_args(*h, ts);
-          const double   fac = A.out_scale;
-          const bool     last = st == ns - 1;
-          A.gauss             = gauss;
-          if (traces)
-            {
-              A.tr_in  = tr_in;
-              A.tr_out = tr_out;
-              std::swap(tr_in, tr_out);
-            }
-          A.b                 = bi[st] * dt * fac;
-          A.a                 = last ? 0.0 : ai[st] * dt * fac;
-          A.mode              = last ? adv::kModeLastStage : adv::kModeStage;
-          if (st == 0)
-            {
-              A.r_in = u, A.u_in = u, A.u_out = k, A.r_out = r;
-            }
-          else if (st == 1)
-            {
-              A.r_in = r, A.u_in = k, A.u_out = u, A.r_out = k;
-            }
-          else
-            {
-              double *rin  = (st % 2 == 0) ? k : r;
-              double *rout = (st % 2 == 0) ? r : k;
-              A.r_in = rin, A.u_in = u, A.u_out = u, A.r_out = last ? nullptr : rout;
-            }
-          if (int e = launch(h, A, s))
-            return e;
-        }
-    }
-  if (gauss)
-    {
-      ADV_CUDA(adv::launch_basis_change(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, false, s));
-      ++h->launches;
-    }
-  return ADV_OK;
+  return run_steps(h, n_steps, ns, gauss, traces, u, host, s, [&](int step, int st, adv::StageArgs &A, int &prec) {
+    return plain_stage(h, ai, bi, t, dt, step, st, gauss, traces, u, r, k, A, prec);
+  });
+}
+} // namespace
+} // extern "C++"
+
+int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, double *u, double *r,
+                   double *k, void *stream)
+{
+  adv::detail::CallTrace trace_(h, "adv_lsrk_steps", (cudaStream_t)stream);
+  return lsrk_steps_impl(h, scheme, t, dt, n_steps, u, r, k, nullptr, (cudaStream_t)stream);
+}
+
+int adv_lsrk_steps_host(adv_handle *h, int scheme, double t, double dt, int n_steps, double *u_host, double *u,
+                        double *r, double *k, void *stream)
+{
+  adv::detail::CallTrace trace_(h, "adv_lsrk_steps_host", (cudaStream_t)stream);
+  if (!u_host)
+    return fail(ADV_ERR_INVALID, "null argument");
+  return lsrk_steps_impl(h, scheme, t, dt, n_steps, u, r, k, u_host, (cudaStream_t)stream);
 }
 
 int adv_lsrk_step(adv_handle *h, int scheme, double t, double dt, double *u, double *r, double *k,

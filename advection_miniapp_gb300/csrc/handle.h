@@ -44,6 +44,10 @@ struct adv_handle
   double                                          timed_seconds = 0.0;
   int64_t                                         timed_calls   = 0;
   int                                             trace_depth   = 0; // entry points nested in a traced call
+  // adv_lsrk_steps_host: copy streams (host -> device, device -> host) and
+  // the events that order the chunked copies against the stage launches
+  cudaStream_t             copy_stream[2] = {};
+  std::vector<cudaEvent_t> pipe_events;
 };
 
 

@@ -12,11 +12,12 @@ Our arm prints one JSON line: `value` is the FP64 operator's whole-job
 GDoF/s per stage with all data resident in HBM (three 262 MB vectors plus the
 geometry, larger than the 129 MB L2, so no flush is needed); `fp32_operator`
 holds the FP32-operator path (FP64 vectors) with its L2 error next to the FP64
-one; `e2e` repeats the FP64 measurement through the public Python API with a
-pinned-host -> device copy of the solution before and a device -> host copy
-after every step; `roofline` and `cpu_baseline` explain the numbers.  With
---gpus N > 1 (torchrun) every rank solves its own replica (the path has no
-data exchange between independent solves): weak scaling.
+one; `e2e` repeats the FP64 measurement through the C ABI's host-buffer entry
+point (adv_lsrk_steps_host), which copies the solution from pinned host memory
+to the device and back around every step; `roofline` and `cpu_baseline`
+explain the numbers.  With --gpus N > 1 (torchrun) every rank solves its own
+replica (the path has no data exchange between independent solves): weak
+scaling.
 
 The reference arm (--impl reference) times the CPU oracle, the FP64 C++
 restatement of the reference's algorithm (the deal.II reference cannot be
@@ -44,7 +45,7 @@ STAGES = 5
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -160,6 +161,10 @@ class ClockSampler:
                  "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # the timed region starts once the sampler is running
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 3.0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
@@ -230,7 +235,7 @@ def reference_arm(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    res = oracle_run(args.steps, args.warmup)
+    res = oracle_run(args.steps, args.warmup, time_budget=120.0)
     sample = (f"{res['steps']} full LSRK(5,4) steps of the {WORKLOAD} workload after {args.warmup} warm-up "
               f"steps, {res['seconds']:.1f} s")
     line = {
@@ -280,9 +285,11 @@ def run_precision(torch, adv, precision, args, stream, sampler_index):
 
 
 def e2e_fp64(torch, adv, args, stream):
-    """FP64 through the public API with host copies of the solution around every step."""
+    """FP64 through the C ABI with the solution in pinned host memory: every
+    step is one adv_lsrk_steps_host call, which copies the solution in, runs
+    the step and copies it back (the copies in chunks of z layers, overlapped
+    with the first and the last stage)."""
     op = adv.AdvectionOperation(adv.workload_config(WORKLOAD))
-    integ = adv.LowStorageRungeKuttaIntegrator(adv.LSRK_5_4)
     dt = op.time_step(0.5)
     u = op.initialize_dof_vector()
     op.project_initial(u)
@@ -292,9 +299,7 @@ def e2e_fp64(torch, adv, args, stream):
     nb = op.n_dofs * 8
 
     def step(t):
-        u.copy_(host, non_blocking=True)
-        integ.perform_time_step(op, t, dt, u, r, k, stream=stream)
-        host.copy_(u, non_blocking=True)
+        op.lsrk_steps_host(adv.LSRK_5_4, t, dt, 1, host, u, r, k, stream=stream)
 
     with torch.cuda.stream(stream):
         for s in range(args.warmup):

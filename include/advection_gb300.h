@@ -164,6 +164,17 @@ int adv_lsrk_step(adv_handle *h, int scheme, double t, double dt, double *u, dou
  * without output). */
 int adv_lsrk_steps(adv_handle *h, int scheme, double t, double dt, int n_steps, double *u,
                    double *r, double *k, void *stream);
+/* adv_lsrk_steps on a solution in host memory (the reference's time loop
+ * with its vectors in host memory, advection_solver.cc:1275-1300): u_host
+ * (n_dofs values; page-locked for the copies to overlap) is copied into the
+ * device vector u, advanced by n_steps steps and copied back.  The copies run
+ * on two copy streams of the handle in chunks of z layers, overlapped with the
+ * first stage (host -> device) and the last stage (device -> host); the
+ * results are those of adv_lsrk_steps bit for bit.  u_host must stay
+ * untouched until the stream has passed the call, and then holds the result;
+ * u holds it too. */
+int adv_lsrk_steps_host(adv_handle *h, int scheme, double t, double dt, int n_steps, double *u_host,
+                        double *u, double *r, double *k, void *stream);
 /* Number of stages and the (a, b) coefficients of a scheme (a has n_stages-1 entries). */
 int adv_lsrk_coefficients(int scheme, double *a, double *b, int *n_stages);
 

@@ -83,6 +83,7 @@ def test_null_arguments(adv_lib):
     assert L.adv_create(None, None) == 1
     assert L.adv_apply(None, None, None, 0.0, None) == 1
     assert L.adv_lsrk_steps(None, 1, 0.0, 0.1, 1, None, None, None, None) == 1
+    assert L.adv_lsrk_steps_host(None, 1, 0.0, 0.1, 1, None, None, None, None, None) == 1
     assert L.adv_destroy(None) == 0
 
 
