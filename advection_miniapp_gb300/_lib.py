@@ -45,7 +45,8 @@ class AdvConfig(ctypes.Structure):
         ("ic_params", ctypes.c_double * 8),
         ("precision", ctypes.c_int32),
         ("fused_form", ctypes.c_int32),
-        ("reserved1", ctypes.c_int32 * 6),
+        ("anchor_interval", ctypes.c_int32),
+        ("reserved1", ctypes.c_int32 * 5),
     ]
 
 

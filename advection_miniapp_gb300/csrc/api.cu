@@ -180,6 +180,8 @@ int validate(const adv_config &c)
     return fail(ADV_ERR_INVALID, "degree must be in 1..6");
   if (c.fused_form < ADV_FORM_AUTO || c.fused_form > ADV_FORM_COLLOCATION_NO_TRACES)
     return fail(ADV_ERR_INVALID, "unknown fused_form");
+  if (c.anchor_interval < 0 || c.anchor_interval > 64)
+    return fail(ADV_ERR_INVALID, "anchor_interval must be in 0..64");
   for (int d = 0; d < 3; ++d)
     {
       if (c.n_cells[d] < 1)
@@ -906,39 +908,54 @@ int plain_stage(adv_handle *h, const std::vector<double> &ai, const std::vector<
   return ADV_OK;
 }
 
-// FP32 increments (ADV_PRECISION_FP32_INCREMENT): per step, stage 0 with the
-// FP64 operator writes K0 = L(u_n), E = b0 dt K0 and G = a0 dt K0 (the
-// increments u - u_n and r - u_n); stages s >= 1 evaluate k = K0 + L32(G_s)
-// and update E and G in FP64; the last stage writes u_n + E + b dt k into u.
-// Buffers: E = r, G alternates between k and a handle scratch vector, K0 in
-// a second scratch vector.
+// FP32 increments (ADV_PRECISION_FP32_INCREMENT).  Steps come in blocks of
+// m = anchor_interval steps.  The first stage of a block's first step runs
+// the FP64 operator on the block's start value B (= u) and writes K0 = L(B),
+// E = b0 dt K0 and G = a0 dt K0, the increments u - B and r - B.  Every other
+// stage of the block evaluates k = K0 + L32(G) with the FP32 operator and
+// updates E and G in FP64.  The first stage of a later step of the block
+// takes G = E (the step's start value relative to B).  The last stage of the
+// block writes B + E + b dt k into u; the last stage of the block's other
+// steps only updates E.  Buffers: u holds B, K0 a scratch vector, and E and
+// the two G registers rotate over r, k and a second scratch vector: in the
+// block's step j, E is in P[j % 3] and G in P[(j + 1) % 3], P[(j + 2) % 3].
 int increment_stage(adv_handle *h, const std::vector<double> &ai, const std::vector<double> &bi, double t,
-                    double dt, int step, int st, bool gauss, double *u, double *r, double *k, adv::StageArgs &A,
-                    int &prec)
+                    double dt, int n_steps, int step, int st, bool gauss, double *u, double *r, double *k,
+                    adv::StageArgs &A, int &prec)
 {
   const int ns = (int)bi.size();
-  double   *E = r, *Ga = k, *Gb = h->d_scratch[0], *K0 = h->d_scratch[1];
-  prec            = st == 0 ? 0 : 1;
-  A               = base_args(*h, stage_time(ai, bi, t + step * dt, dt, st), prec);
-  const bool last = st == ns - 1;
-  A.gauss         = gauss;
-  A.b             = bi[st] * dt * A.out_scale;
-  A.a             = last ? 0.0 : ai[st] * dt * A.out_scale;
-  A.mode          = last ? adv::kModeLastStage : adv::kModeStage;
-  if (st == 0)
+  const int m  = h->cfg.anchor_interval > 0 ? h->cfg.anchor_interval : 4;
+  const int j  = step % m;
+  double   *P[3] = {r, k, h->d_scratch[0]}, *K0 = h->d_scratch[1];
+  double   *E = P[j % 3], *Ga = P[(j + 1) % 3], *Gb = P[(j + 2) % 3];
+  const bool anchor = j == 0 && st == 0;
+  prec              = anchor ? 0 : 1;
+  A                 = base_args(*h, stage_time(ai, bi, t + step * dt, dt, st), prec);
+  const bool last   = st == ns - 1;
+  A.gauss           = gauss;
+  A.b               = bi[st] * dt * A.out_scale;
+  A.a               = last ? 0.0 : ai[st] * dt * A.out_scale;
+  A.mode            = last ? adv::kModeLastStage : adv::kModeStage;
+  if (anchor)
     {
       A.r_in = u, A.u_in = nullptr, A.u_out = E, A.r_out = Ga, A.k_out = K0;
+      return ADV_OK;
     }
-  else
+  A.k_add = K0;
+  if (st == 0)
     {
-      A.r_in  = (st % 2) ? Ga : Gb;
-      A.k_add = K0;
-      A.u_in  = E;
-      if (last)
-        A.u_out = u, A.u_base = u;
-      else
-        A.u_out = E, A.r_out = (st % 2) ? Gb : Ga;
+      // E of the previous step (in P[(j - 1) % 3] = Gb) is this step's start
+      A.r_in = Gb, A.u_in = Gb, A.u_out = E, A.r_out = Ga;
+      return ADV_OK;
     }
+  A.r_in = (st % 2) ? Ga : Gb;
+  A.u_in = E;
+  if (!last)
+    A.u_out = E, A.r_out = (st % 2) ? Gb : Ga;
+  else if (j == m - 1 || step == n_steps - 1)
+    A.u_out = u, A.u_base = u;
+  else
+    A.u_out = E;
   return ADV_OK;
 }
 
@@ -1177,7 +1194,7 @@ int lsrk_steps_impl(adv_handle *h, int scheme, double t, double dt, int n_steps,
       const bool gauss = n_steps > 0 && h->cfg.fused_form != ADV_FORM_NODAL;
       return run_steps(h, n_steps, ns, gauss, false, u, host, s,
                        [&](int step, int st, adv::StageArgs &A, int &prec) {
-                         return increment_stage(h, ai, bi, t, dt, step, st, gauss, u, r, k, A, prec);
+                         return increment_stage(h, ai, bi, t, dt, n_steps, step, st, gauss, u, r, k, A, prec);
                        });
     }
   // collocation form: the solution moves to the Gauss-point values for the

@@ -43,7 +43,9 @@ def parse(argv=None):
     p.add_argument("--scheme", choices=sorted(SCHEMES), default="5_4")
     p.add_argument("--precision", choices=["fp64", "fp32", "fp32-increment"], default="fp64",
                    help="FP64 operator, FP32 operator, or FP32 operator on the stage increments with one FP64 "
-                        "evaluation per step")
+                        "evaluation per anchor interval")
+    p.add_argument("--anchor-interval", type=int, default=0,
+                   help="fp32-increment: steps per FP64 anchor evaluation (0: the library default, 4)")
     p.add_argument("--form", choices=["auto", "nodal", "collocation", "collocation-no-traces"], default="auto",
                    help="basis of the stages inside the fused step loop (fused_form)")
     p.add_argument("--flux-alpha", type=float, default=1.0)
@@ -114,6 +116,7 @@ def main(argv=None):
                           deformation=args.deformation if args.mesh == "deformed" else 0.0,
                           velocity=tuple(args.velocity), initial_condition=ICS[args.initial_condition],
                           flux_alpha=args.flux_alpha, factor_skew=args.skew, precision=precision)
+    cfg.anchor_interval = args.anchor_interval
     cfg.fused_form = {"auto": FORM_AUTO, "nodal": FORM_NODAL, "collocation": FORM_COLLOCATION,
                       "collocation-no-traces": FORM_COLLOCATION_NO_TRACES}[args.form]
     op = AdvectionOperation(cfg)

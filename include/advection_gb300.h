@@ -49,12 +49,14 @@ enum { ADV_VELOCITY_CONSTANT = 0, ADV_VELOCITY_ROTATING = 1 };
 enum { ADV_IC_SINE_GAUSS = 0, ADV_IC_BLOB = 1, ADV_IC_WAVE = 2 };
 enum { ADV_BOUNDARY_ZERO = 0, ADV_BOUNDARY_EXACT = 1 };
 /* FP32_INCREMENT: the FP32 operator on stage increments.  In adv_lsrk_steps
- * every step evaluates L(u_n) once with the FP64 operator and the other
- * stages as L(u_n) + L32(r_s - u_n), where r_s - u_n = O(dt |L u|) is carried
- * in FP64 (exact for linear operators that do not depend on time: constant
- * velocity, periodic or zero Dirichlet data).  The FP32 round-off then scales
- * with the increment instead of the solution.  Elsewhere (apply,
- * perform_stage, other operators) it is the FP32 operator. */
+ * every anchor_interval-th step evaluates L(u_a) at its start u_a with the
+ * FP64 operator, and every other stage until the next anchor evaluates
+ * L(u_a) + L32(r_s - u_a), where r_s - u_a = O(j dt |L u|) (j steps after the
+ * anchor) is carried in FP64 (exact for linear operators that do not depend
+ * on time: constant velocity, periodic or zero Dirichlet data).  The FP32
+ * round-off then scales with the increment instead of the solution.
+ * Elsewhere (apply, perform_stage, other operators) it is the FP32
+ * operator. */
 enum { ADV_PRECISION_FP64 = 0, ADV_PRECISION_FP32_OPERATOR = 1, ADV_PRECISION_FP32_INCREMENT = 2 };
 /* LSRK schemes in the order of the reference's enum (advection_solver.cc:83-89) */
 enum { ADV_LSRK_3_3 = 0, ADV_LSRK_5_4 = 1, ADV_LSRK_7_4 = 2, ADV_LSRK_9_5 = 3 };
@@ -99,7 +101,8 @@ typedef struct adv_config
   /* ---- fields below have no counterpart in the oracle's configuration ---- */
   int32_t precision;         /* ADV_PRECISION_*: FP64, FP32 operator with FP64 vectors, FP32 increments */
   int32_t fused_form;        /* ADV_FORM_*: basis of the stages inside adv_lsrk_steps */
-  int32_t reserved1[6];
+  int32_t anchor_interval;   /* FP32 increments: steps per FP64 anchor evaluation, 1..64 (0: 4) */
+  int32_t reserved1[5];
 } adv_config;
 
 typedef struct adv_handle adv_handle;

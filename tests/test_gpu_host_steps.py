@@ -51,6 +51,7 @@ def _run_both(torch, adv, cfg, precision, n_steps, scheme, form=None):
     host.copy_(u0.cpu())
     ud, rd, kd = op.initialize_dof_vector(), op.initialize_dof_vector(), op.initialize_dof_vector()
     ud.fill_(7.0)
+    torch.cuda.synchronize()
     s = torch.cuda.Stream()
     with torch.cuda.stream(s):
         op.lsrk_steps_host(scheme, 0.1, dt, n_steps, host, ud, rd, kd, stream=s)
@@ -106,6 +107,7 @@ def test_host_steps_back_to_back_calls(cuda, adv_lib):
     op.lsrk_steps(adv.LSRK_5_4, 0.0, dt, 4, u, r, k)
     host = u0.cpu().pin_memory()
     ud, rd, kd = op.initialize_dof_vector(), op.initialize_dof_vector(), op.initialize_dof_vector()
+    torch.cuda.synchronize()
     s = torch.cuda.Stream()
     with torch.cuda.stream(s):
         for i in range(4):
