@@ -690,6 +690,7 @@ int adv_destroy(adv_handle *h)
     }
   cudaFree(h->d_traces[0]);
   cudaFree(h->d_traces[1]);
+  cudaFree(h->d_inc32);
   for (cudaEvent_t e : h->pipe_events)
     cudaEventDestroy(e);
   for (cudaStream_t cs : h->copy_stream)
@@ -959,6 +960,82 @@ int increment_stage(adv_handle *h, const std::vector<double> &ai, const std::vec
   return ADV_OK;
 }
 
+// FP32 increments in the collocation form, with the anchor's K0 folded out
+// of the FP64 registers.  Within a block, with C the sum of the b dt of the
+// stages since the anchor, the kernels carry e = u - u_a - C K0 (FP64) and
+// the next operator input G = r - u_a only in binary32 (the FP32 operator
+// reads nothing finer), which with k = K0 + kh, kh = L32(G), turns
+//   E' = E + b k,  G' = E + a k    into    e' = e + b kh,  G' = e + (C + a) K0 + a kh
+// with K0 read in binary32 for G' and in FP64 once, at the end of the block:
+//   u = u_a + e + b kh + (C + b) K0.
+// The anchor writes K0 (FP64 and binary32) and G = a0 dt K0; e starts at 0.
+// A stage reads 4 + 8 + 4 and writes 8 + 4 bytes per DoF instead of 24 + 16,
+// and issues one FP64 instruction per DoF instead of two.  The last stage of
+// a step inside a block writes the next step's start G = e' + (C + b) K0.
+// Buffers: u holds u_a, K0 a scratch vector, e lives in r; the two G
+// registers and K0 in binary32 share one allocation of 3 n_dofs floats.
+int increment_stage_folded(adv_handle *h, const std::vector<double> &ai, const std::vector<double> &bi, double t,
+                           double dt, int n_steps, int step, int st, double *u, double *r, adv::StageArgs &A,
+                           int &prec)
+{
+  const int ns     = (int)bi.size();
+  const int m      = h->cfg.anchor_interval > 0 ? h->cfg.anchor_interval : 4;
+  const int j      = step % m;
+  const int q      = j * ns + st; // stage index inside the block
+  const int64_t nd = h->mesh.n_dofs;
+  float    *G[2]   = {h->d_inc32, h->d_inc32 + nd}, *K32 = h->d_inc32 + 2 * nd;
+  double   *K0     = h->d_scratch[1];
+  prec             = q == 0 ? 0 : 1;
+  A                = base_args(*h, stage_time(ai, bi, t + step * dt, dt, st), prec);
+  A.gauss          = true;
+  A.inc32          = 1;
+  A.mode           = adv::kModeStage;
+  if (q == 0)
+    {
+      A.r_in  = u;
+      A.a     = ai[0] * dt * A.out_scale;
+      A.k_out = K0, A.k_out32 = K32, A.r_out32 = G[0];
+      return ADV_OK;
+    }
+  // C: the b dt of the stages since the anchor, summed in stage order
+  double C = 0.0;
+  for (int p = 0; p < q; ++p)
+    C += bi[p % ns] * dt * A.out_scale;
+  const bool last_of_step  = st == ns - 1;
+  const bool last_of_block = last_of_step && (j == m - 1 || step == n_steps - 1);
+  A.b       = bi[st] * dt * A.out_scale;
+  A.r_in32  = G[(q - 1) & 1];
+  A.u_in    = q == 1 ? nullptr : r;
+  A.u_out   = r;
+  if (last_of_block)
+    {
+      A.mode      = adv::kModeLastStage;
+      A.inc_alpha = C + A.b;
+      A.k_add     = K0;
+      A.u_base    = u;
+      A.u_out     = u;
+      return ADV_OK;
+    }
+  // inside a step: G' = e + (C + a) K0 + a kh; at the end of a step: the
+  // next step's start, e' + (C + b) K0 = e + (C + b) K0 + b kh
+  const double a = last_of_step ? A.b : ai[st] * dt * A.out_scale;
+  A.inc_af       = (float)a;
+  A.inc_alphaf   = (float)(C + a);
+  A.k_add32      = K32;
+  A.r_out32      = G[q & 1];
+  return ADV_OK;
+}
+
+int ensure_inc32(adv_handle *h)
+{
+  if (!h->d_inc32)
+    {
+      ADV_CUDA(cudaMalloc(&h->d_inc32, 3 * h->mesh.n_dofs * sizeof(float)));
+      h->device_bytes += 3 * h->mesh.n_dofs * (int64_t)sizeof(float);
+    }
+  return ADV_OK;
+}
+
 // the increment form is exact for operators linear in u and independent of
 // time: constant velocity, no inhomogeneous (exact) Dirichlet data
 bool increment_form_applies(const adv_handle &h)
@@ -1192,6 +1269,15 @@ int lsrk_steps_impl(adv_handle *h, int scheme, double t, double dt, int n_steps,
       if (int e = ensure_scratch(h, 1))
         return e;
       const bool gauss = n_steps > 0 && h->cfg.fused_form != ADV_FORM_NODAL;
+      if (gauss)
+        {
+          if (int e = ensure_inc32(h))
+            return e;
+          return run_steps(h, n_steps, ns, true, false, u, host, s,
+                           [&](int step, int st, adv::StageArgs &A, int &prec) {
+                             return increment_stage_folded(h, ai, bi, t, dt, n_steps, step, st, u, r, A, prec);
+                           });
+        }
       return run_steps(h, n_steps, ns, gauss, false, u, host, s,
                        [&](int step, int st, adv::StageArgs &A, int &prec) {
                          return increment_stage(h, ai, bi, t, dt, n_steps, step, st, gauss, u, r, k, A, prec);

@@ -31,6 +31,7 @@ struct adv_handle
   double  *d_partials    = nullptr;
   double  *d_scratch[2]  = {};
   void    *d_traces[2]   = {}; // face traces of the collocation step loop (lazily allocated)
+  float   *d_inc32       = nullptr; // FP32 increments: two G registers and K0 in binary32 (lazily)
   int64_t  device_bytes  = 0;
   int64_t  launches      = 0;
   adv::DiagArgs diag;

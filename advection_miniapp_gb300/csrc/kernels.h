@@ -68,6 +68,22 @@ struct StageArgs
   const double *k_add;
   double       *k_out;
   const double *u_base;
+  // FP32 increments with the anchor's k folded out (collocation form, inc32
+  // != 0; K0 = L(u_a) of the block's FP64 anchor, e = u_in the increment
+  // u - u_a - C K0 with C the sum of the b's since the anchor):
+  //   stage:  u_out = e + b k;  r_out32 = binary32(e + inc_alpha K0 + a k)
+  //           (k_add32 holds K0; the anchor itself, run by the FP64 kernel
+  //           on u_a, writes k_out = K0, k_out32 = binary32(K0) and
+  //           r_out32 = binary32(a K0) and nothing else);
+  //   last:   u_out = u_base + (e + b k) + inc_alpha K0 (k_add holds K0)
+  // r_in32 replaces r_in as the operator's input.
+  int           inc32;
+  float         inc_alphaf, inc_af;
+  double        inc_alpha;
+  const float  *r_in32;
+  float        *r_out32;
+  const float  *k_add32;
+  float        *k_out32;
   ExactParams   ex;
 };
 

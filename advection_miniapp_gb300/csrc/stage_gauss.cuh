@@ -67,7 +67,11 @@ struct GaussShape
   static_assert(GB_OFFSET % 16 == 0, "cp.async destinations need 16-byte alignment");
 };
 
-template <int N, typename T, bool UNI, bool VISC, bool TR = false>
+// INC: FP32 increments with the anchor's K0 folded out (StageArgs::inc32).
+// Binary32 operator: the input comes from r_in32 and the update is the
+// increment form's.  FP64 operator: the block's anchor (writes K0 and the
+// first G).
+template <int N, typename T, bool UNI, bool VISC, bool TR = false, bool INC = false>
 __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long long cell0,
                                                 unsigned char *smem_raw)
 {
@@ -105,6 +109,10 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
             asm volatile("prefetch.global.L2 [%0];" ::"l"(reinterpret_cast<const char *>(base + cell0 * NQ) +
                                                           128 * (i % lines)));
         }
+      if (INC && sizeof(T) == sizeof(float) && A.k_add32)
+        for (int i = tid; i < (ncell * NQ * (int)sizeof(float) + 127) / 128; i += NT)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(reinterpret_cast<const char *>(A.k_add32 + cell0 * NQ) +
+                                                        128 * i));
     }
   cell_neighbours(A, cell0, ncell, s_nbr, s_face, tid, NT);
   __syncthreads();
@@ -131,9 +139,18 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
   // ---- phase 1: own values (one contiguous range of the CTA's cells) and
   //      the neighbours' values at the face points
   {
-    const double *src = A.r_in + cell0 * NQ;
-    for (int i = tid; i < ncell * NQ; i += NT)
-      Ub[i] = from_double<T>(__ldg(src + i));
+    if (INC && sizeof(T) == sizeof(float))
+      {
+        const float *src = A.r_in32 + cell0 * NQ;
+        for (int i = tid; i < ncell * NQ; i += NT)
+          Ub[i] = T(__ldg(src + i));
+      }
+    else
+      {
+        const double *src = A.r_in + cell0 * NQ;
+        for (int i = tid; i < ncell * NQ; i += NT)
+          Ub[i] = from_double<T>(__ldg(src + i));
+      }
     if (TR)
       {
         const T *tr = static_cast<const T *>(A.tr_in) + cell0 * 6 * TRW * NF;
@@ -161,12 +178,21 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
           // with its basis at the shared face: xi_d = 1 for the neighbour
           // below (low face, j even), xi_d = 0 for the one above
           const T      *l  = (j & 1) ? tb.l0 : tb.l1;
-          const int     sd = d == 0 ? 1 : d == 1 ? N : NF;
-          const double *g  = A.r_in + (long long)nb * NQ + idx3<N>(d, 0, fq % N, fq / N);
-          T             v[N];
+          const int       sd  = d == 0 ? 1 : d == 1 ? N : NF;
+          const long long off = (long long)nb * NQ + idx3<N>(d, 0, fq % N, fq / N);
+          T               v[N];
+          if (INC && sizeof(T) == sizeof(float))
+            {
 #pragma unroll
-          for (int a = 0; a < N; ++a)
-            v[a] = from_double<T>(__ldg(g + a * sd));
+              for (int a = 0; a < N; ++a)
+                v[a] = T(__ldg(A.r_in32 + off + a * sd));
+            }
+          else
+            {
+#pragma unroll
+              for (int a = 0; a < N; ++a)
+                v[a] = from_double<T>(__ldg(A.r_in + off + a * sd));
+            }
           T s = l[0] * v[0];
 #pragma unroll
           for (int a = 1; a < N; ++a)
@@ -276,6 +302,31 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
             zz *= G[3 * NQ + r + k * NF];
           const long long gi = gb + k * NF;
           double          kd = to_double<T>(zz);
+          if (INC)
+            {
+              // FP32 increments with the anchor's K0 folded out
+              next[k] = 0.0;
+              if constexpr (sizeof(T) == sizeof(double))
+                {
+                  // the block's FP64 anchor on u_a: K0 and the first G
+                  A.k_out[gi]   = kd;
+                  A.k_out32[gi] = d2f_int(kd);
+                  A.r_out32[gi] = d2f_int(A.a * kd);
+                }
+              else if (A.mode == kModeStage)
+                {
+                  const double e = A.u_in ? __ldcs(A.u_in + gi) : 0.0;
+                  A.u_out[gi]    = fma(A.b, kd, e);
+                  A.r_out32[gi]  = fmaf(A.inc_alphaf, __ldcs(A.k_add32 + gi), fmaf(A.inc_af, float(zz), d2f_int(e)));
+                }
+              else
+                {
+                  double un   = fma(A.b, kd, A.u_in ? __ldcs(A.u_in + gi) : 0.0);
+                  un          = fma(A.inc_alpha, __ldcs(A.k_add + gi), un);
+                  A.u_out[gi] = un + __ldcs(A.u_base + gi);
+                }
+              continue;
+            }
           if (!TR && A.k_add)
             kd += __ldcs(A.k_add + gi);
           if (A.mode == kModeStage)
@@ -355,15 +406,15 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
     }
 }
 
-template <int N, typename T, bool UNI, bool VISC, bool TR>
+template <int N, typename T, bool UNI, bool VISC, bool TR, bool INC>
 __global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS) stage_gauss_kernel(const StageArgs A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_gauss_cta<N, T, UNI, VISC, TR>(A, A.cell_begin + (long long)blockIdx.x * StageShape<N, T, UNI, VISC>::C,
+  stage_gauss_cta<N, T, UNI, VISC, TR, INC>(A, A.cell_begin + (long long)blockIdx.x * StageShape<N, T, UNI, VISC>::C,
                                        smem_raw);
 }
 
-template <int N, typename T, bool UNI, bool VISC, bool TR>
+template <int N, typename T, bool UNI, bool VISC, bool TR, bool INC = false>
 cudaError_t launch_stage_gauss_t(const StageArgs &args, cudaStream_t stream)
 {
   using GS = GaussShape<N, T, UNI, VISC, TR>;
@@ -374,7 +425,7 @@ cudaError_t launch_stage_gauss_t(const StageArgs &args, cudaStream_t stream)
     return e;
   if (dev >= 64 || !((configured >> dev) & 1ull))
     {
-      e = cudaFuncSetAttribute(stage_gauss_kernel<N, T, UNI, VISC, TR>,
+      e = cudaFuncSetAttribute(stage_gauss_kernel<N, T, UNI, VISC, TR, INC>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, GS::SMEM);
       if (e != cudaSuccess)
         return e;
@@ -382,7 +433,7 @@ cudaError_t launch_stage_gauss_t(const StageArgs &args, cudaStream_t stream)
         configured |= 1ull << dev;
     }
   const long long blocks = (args.n_cells - args.cell_begin + GS::C - 1) / GS::C;
-  stage_gauss_kernel<N, T, UNI, VISC, TR><<<(unsigned)blocks, GS::THREADS, GS::SMEM, stream>>>(args);
+  stage_gauss_kernel<N, T, UNI, VISC, TR, INC><<<(unsigned)blocks, GS::THREADS, GS::SMEM, stream>>>(args);
   return cudaGetLastError();
 }
 
@@ -395,6 +446,10 @@ cudaError_t launch_stage_gauss_n(const StageArgs &args, cudaStream_t stream)
       return args.visc ? launch_stage_gauss_t<N, T, false, true, true>(args, stream)
            : args.uniform ? launch_stage_gauss_t<N, T, true, false, true>(args, stream)
                           : launch_stage_gauss_t<N, T, false, false, true>(args, stream);
+  if (args.inc32)
+    return args.visc ? launch_stage_gauss_t<N, T, false, true, false, true>(args, stream)
+         : args.uniform ? launch_stage_gauss_t<N, T, true, false, false, true>(args, stream)
+                        : launch_stage_gauss_t<N, T, false, false, false, true>(args, stream);
   if (args.visc)
     return launch_stage_gauss_t<N, T, false, true, false>(args, stream);
   return args.uniform ? launch_stage_gauss_t<N, T, true, false, false>(args, stream)

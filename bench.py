@@ -461,9 +461,9 @@ def ours(args):
             "value": round(vinc, 4), "unit": "GDoF/s", "speedup_vs_fp64": round(vinc / v64, 3),
             "rel_l2_error": rinc["rel_l2"], "l2_error_ratio": round(rinc["rel_l2"] / r64["rel_l2"], 6),
             "ms_per_step": round(secinc / args.steps * 1e3, 4),
-            "form": "per 4 steps (anchor_interval 4) one FP64 operator evaluation L(u_a) at the block's start "
-                    "u_a and 19 FP32 operator evaluations on the increments r - u_a kept in FP64; collocation "
-                    "basis",
+            "form": "per 4 steps (anchor_interval 4) one FP64 operator evaluation K0 = L(u_a) at the block's "
+                    "start u_a and 19 FP32 operator evaluations on the increments r - u_a (u - u_a - C K0 kept in "
+                    "FP64, the operator input in binary32); collocation basis",
             "clocks": rinc["clocks"]},
         "e2e": e2e,
         "gpu_launches": r64["launches"] + r32["launches"] + rinc["launches"],

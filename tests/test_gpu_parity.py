@@ -353,8 +353,8 @@ def test_fp32_increment_form_falls_back_for_time_dependent_operators(cuda, oracl
 def test_fp32_increment_l2_error_equals_fp64_at_fine_resolution(cuda, adv_lib):
     """32^3 curved cells of degree 4, 40 steps: the increment form, anchored
     every step or every 4 steps (the default), matches FP64 within 1.05x.
-    Measured: 1.0000 / 1.0003 at 32^3, 1.0007 / 1.008 at 64^3 and 1.0008 /
-    1.014 at 128^3."""
+    Measured: 1.0001 / 1.0004 at 32^3, 1.0007 / 1.0097 at 64^3 and 1.0009 /
+    1.018 at 128^3."""
     errs = {}
     for precision, interval in ((0, 0), (2, 1), (2, 0)):
         g = adv_lib.AdvectionOperation(adv_lib.workload_config("deformed-k4-32", precision=precision,
