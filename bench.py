@@ -124,6 +124,19 @@ def fp_work_per_cell(n, curved=True, stage=True, collocation=False, traces=False
 NCU_TRAFFIC_PER_DOF = {"fp64": (542.872064e6 + 175.501312e6) / 8.0e6, "fp32": (296.930816e6 + 94.676992e6) / 8.0e6}
 
 
+def increment_bytes_per_dof_step(n, interval=4, stages=STAGES):
+    """Algorithmic DRAM bytes per DoF and step of the FP32 increment form in
+    collocation (anchor every `interval` steps): the FP64 anchor reads u_a and
+    writes K0 (FP64), K0 and G (binary32) with FP64 geometry; the first FP32
+    stage reads G and K0 (binary32) and writes e (FP64) and G; the others read
+    G, e, K0 and write e, G; the block's last stage reads G, e, K0 (FP64) and
+    u_a and writes u; every FP32 stage reads the binary32 geometry."""
+    q = interval * stages
+    vec = (8 + 8 + 4 + 4) + (4 + 4 + 8 + 4) + (q - 3) * (4 + 8 + 4 + 8 + 4) + (4 + 8 + 8 + 8 + 8)
+    geo = geometry_bytes_per_dof(n, 8) + (q - 1) * geometry_bytes_per_dof(n, 4)
+    return (vec + geo) / interval
+
+
 def traffic(per_dof, n_dofs):
     """DRAM bytes of one stage launch of the workload from the ncu figure per DoF."""
     return None if per_dof is None else round(per_dof * n_dofs)
@@ -406,6 +419,7 @@ def ours(args):
     peaks_file = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_file):
         hbm_peak = json.load(open(peaks_file)).get("hbm_gbs", hbm_peak)
+    inc_gbs = increment_bytes_per_dof_step(n) * n_dofs / (secinc / args.steps) / 1e9
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -464,6 +478,11 @@ def ours(args):
             "form": "per 4 steps (anchor_interval 4) one FP64 operator evaluation K0 = L(u_a) at the block's "
                     "start u_a and 19 FP32 operator evaluations on the increments r - u_a (u - u_a - C K0 kept in "
                     "FP64, the operator input in binary32); collocation basis",
+            "roofline": {"bound": "hbm", "achieved": round(inc_gbs, 2), "peak": hbm_peak, "unit": "GB/s",
+                         "frac": round(inc_gbs / hbm_peak, 4), "traffic": None,
+                         "bytes_per_dof_step": round(increment_bytes_per_dof_step(n), 2),
+                         "definition": "algorithmic vector and geometry bytes of a 4-step block (one FP64 anchor "
+                                       "and 19 FP32 stages) over the block's time"},
             "clocks": rinc["clocks"]},
         "e2e": e2e,
         "gpu_launches": r64["launches"] + r32["launches"] + rinc["launches"],
