@@ -24,10 +24,11 @@
 // of its output that the next stage reads (r_out, or u_out on a last stage),
 // [6][n^2] per cell, and with SIPG also the reference normal derivatives
 // there ([6][2][n^2]); the next stage then reads its own and its neighbours'
-// face data instead of contracting pencils.  Per cell-stage at
-// degree 4 the producer adds 750 FMAs and the consumer saves 1500; the
-// traces are the same contractions in the same order, so results are
-// bit-identical to the variant without them.
+// face data, one global read per face point in the direction passes,
+// instead of contracting pencils.  Per cell-stage at degree 4 the producer
+// adds 750 FMAs and the consumer saves 1500; the traces are the same
+// contractions in the same order, so results are bit-identical to the
+// variant without them.
 #pragma once
 
 #include "stage_kernel.cuh"
@@ -40,11 +41,22 @@ struct GaussShape
   using SH                     = StageShape<N, T, UNI, VISC>;
   static constexpr int C       = SH::C;
   static constexpr int THREADS = SH::THREADS;
-  // the nodal layout plus, with traces, Tb [C][6][NF] own face values,
-  // padded to 16 bytes: the geometry after it is filled by 16-byte cp.async
   // traces per face point: the value, and with SIPG the reference normal derivative
-  static constexpr int TRW       = VISC ? 2 : 1;
-  static constexpr int TB_VALUES = TR ? (TRW * 6 * C * N * N * (int)sizeof(T) + 15) / 16 * 16 / (int)sizeof(T) : 0;
+  static constexpr int TRW = VISC ? 2 : 1;
+  // TG: traces read from global memory in the direction passes, one read per
+  // face point, instead of being staged (field geometry without SIPG, where
+  // shared memory limits the resident CTAs: 12 C n^2 values less per CTA,
+  // 7 instead of 5 CTAs per SM in FP64 at degree 4, 2.2 % faster on GB300);
+  // the other variants are limited by registers and stage them
+  static constexpr bool TG = TR && !UNI && !VISC;
+  // staged: neighbour values Nb [C][6][NF], own traces Tb [C][6][TRW][NF],
+  // padded so that the cell geometry Gb after them starts on 16 bytes (it is
+  // filled by 16-byte cp.async)
+  static constexpr int NB_VALUES = TG ? 0 : 6 * C * N * N;
+  static constexpr int TB_VALUES =
+    ((2 * C * N * N * N + NB_VALUES + (TR && !TG ? TRW * 6 * C * N * N : 0)) * (int)sizeof(T) + 15) / 16 * 16 /
+      (int)sizeof(T) -
+    (2 * C * N * N * N + NB_VALUES);
   // field geometry with traces: the face coefficients are read from global
   // memory in the direction passes (one read per face point) instead of being
   // staged, which frees 12 C n^2 values of shared memory per CTA (one more
@@ -59,11 +71,12 @@ struct GaussShape
   static constexpr bool FACES_GLOBAL = !UNI && (TR || VISC || sizeof(T) == sizeof(float));
   static constexpr int  FB_VALUES    = UNI || FACES_GLOBAL ? 0 : 12 * C * N * N;
   static constexpr int  GB_VALUES    = UNI || GEO_GLOBAL ? 0 : 4 * C * N * N * N;
-  static constexpr int  SMEM = SH::SMEM + TB_VALUES * (int)sizeof(T) -
-                              (UNI ? 0 : (12 * C * N * N - FB_VALUES + 4 * C * N * N * N - GB_VALUES) *
-                                           (int)sizeof(T));
+  // viscous: Nd [C][6][NF] neighbour normal derivatives
+  static constexpr int  ND_VALUES    = VISC ? 6 * C * N * N : 0;
+  static constexpr int  SMEM         = (2 * C * N * N * N + NB_VALUES + TB_VALUES + GB_VALUES + FB_VALUES + ND_VALUES) *
+                                    (int)sizeof(T) + 12 * C * (int)sizeof(int);
   // byte offset of the cell geometry Gb in the layout of stage_gauss_cta
-  static constexpr int GB_OFFSET = (2 * C * N * N * N + 6 * C * N * N + TB_VALUES) * (int)sizeof(T);
+  static constexpr int GB_OFFSET = (2 * C * N * N * N + NB_VALUES + TB_VALUES) * (int)sizeof(T);
   static_assert(GB_OFFSET % 16 == 0, "cp.async destinations need 16-byte alignment");
 };
 
@@ -82,15 +95,16 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
   constexpr int NT = SH::THREADS;
   T   *Ub     = reinterpret_cast<T *>(smem_raw); // [C][NQ] Gauss-point values of r_in
   T   *Qb     = Ub + C * NQ;                     // [C][NQ] x and y contributions to Z
-  T   *Nb     = Qb + C * NQ;                     // [C][6][NF] neighbour values at the face points
-  T   *Tb     = Nb + C * 6 * NF;                 // traces: [C][6][TRW][NF] own values (and derivatives)
-  T   *Gb     = Tb + GaussShape<N, T, UNI, VISC, TR>::TB_VALUES; // field: [C][4][NQ] cell geometry
   using GS                 = GaussShape<N, T, UNI, VISC, TR>;
   constexpr bool FG        = GS::FACES_GLOBAL;
   constexpr int  TRW       = GS::TRW;
+  constexpr bool TG        = GS::TG;
+  T   *Nb     = Qb + C * NQ;                     // staged: [C][6][NF] neighbour values at the face points
+  T   *Tb     = Nb + GS::NB_VALUES;              // staged traces: [C][6][TRW][NF] own values (and derivatives)
+  T   *Gb     = Tb + GS::TB_VALUES;              // field: [C][4][NQ] cell geometry
   T   *Fb     = Gb + GS::GB_VALUES;              // field: [C][6][2][NF] face coefficients (staged unless FG)
   T   *Nd     = Fb + GS::FB_VALUES;              // viscous: [C][6][NF] neighbour normal derivatives
-  int *s_nbr  = reinterpret_cast<int *>(Nd + (VISC ? C * 6 * NF : 0));
+  int *s_nbr  = reinterpret_cast<int *>(Nd + GS::ND_VALUES);
   int *s_face = s_nbr + C * 6;
 
   const DevTables<T> &tb    = tab<T>(N);
@@ -151,14 +165,14 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
         for (int i = tid; i < ncell * NQ; i += NT)
           Ub[i] = from_double<T>(__ldg(src + i));
       }
-    if (TR)
+    if (TR && !TG)
       {
         const T *tr = static_cast<const T *>(A.tr_in) + cell0 * 6 * TRW * NF;
         for (int i = tid; i < ncell * 6 * TRW * NF; i += NT)
           Tb[i] = __ldg(tr + i);
       }
   }
-  for (int w = tid; w < ncell * 6 * NF; w += NT)
+  for (int w = tid; w < (TG ? 0 : ncell * 6 * NF); w += NT)
     {
       const int cf = w / NF, fq = w % NF;
       const int j = cf % 6, d = j >> 1;
@@ -224,6 +238,49 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
     __pipeline_wait_prior(0);
   __syncthreads();
 
+  // neighbour value and normal derivative at face point r of face j of local
+  // cell cl: staged, or with traces the neighbour's own trace on the shared
+  // face (its face j ^ 1), or the Dirichlet data on a boundary face
+  const T *tr_in = static_cast<const T *>(A.tr_in);
+  auto     nbv   = [&](int cl, int j, int r) -> T {
+    if constexpr (!TG)
+      return Nb[(cl * 6 + j) * NF + r];
+    else
+      {
+        const int nb = s_nbr[cl * 6 + j];
+        if (nb >= 0)
+          return __ldg(tr_in + ((long long)nb * 6 + (j ^ 1)) * TRW * NF + r);
+        double g = 0.0;
+        if (A.bc_exact)
+          {
+            const int     d  = j >> 1;
+            const double *fx = d == 0 ? A.face_x[0] : d == 1 ? A.face_x[1] : A.face_x[2];
+            const double *x  = fx + ((size_t)s_face[cl * 6 + j] * NF + r) * 3;
+            g                = exact_value(A.ex, x[0], x[1], x[2], A.t);
+          }
+        return from_double<T>(g);
+      }
+  };
+  auto nbd = [&](int cl, int j, int r) -> T {
+    if constexpr (!VISC)
+      return T(0);
+    else
+      return Nd[(cl * 6 + j) * NF + r];
+  };
+  auto trv = [&](const T *p, int o) -> T {
+    if constexpr (TG)
+      return __ldg(p + o);
+    else
+      return p[o];
+  };
+  // own traces of face j (value, and with SIPG the normal derivative)
+  auto own_tr = [&](int cl, int j) -> const T * {
+    if constexpr (TG)
+      return tr_in + ((cell0 + cl) * 6 + j) * TRW * NF;
+    else
+      return Tb + (cl * 6 + j) * TRW * NF;
+  };
+
   // ---- phase 2: x-direction terms
   for (int w = tid; w < ncell * NF; w += NT)
     {
@@ -233,14 +290,14 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
 #pragma unroll
       for (int k = 0; k < N; ++k)
         U[k] = p[k];
-      const T *Tr = Tb + cl * 6 * TRW * NF + r;
-      direction_pass<N, T, UNI, VISC, 0, TR>(A, tb, U, Nb[(cl * 6 + 0) * NF + r], Nb[(cl * 6 + 1) * NF + r],
-                                             VISC ? Nd[(cl * 6 + 0) * NF + r] : T(0),
-                                             VISC ? Nd[(cl * 6 + 1) * NF + r] : T(0), s_nbr[cl * 6 + 0] < 0,
+      const T *Tr = TR ? own_tr(cl, 0) + r : nullptr;
+      direction_pass<N, T, UNI, VISC, 0, TR>(A, tb, U, nbv(cl, 0, r), nbv(cl, 1, r),
+                                             nbd(cl, 0, r),
+                                             nbd(cl, 1, r), s_nbr[cl * 6 + 0] < 0,
                                              s_nbr[cl * 6 + 1] < 0, r, faces(cl, 0), faces(cl, 1),
                                              geo(cl) + N * r,
-                                             1, out, TR ? Tr[0] : T(0), TR ? Tr[TRW * NF] : T(0),
-                                             TR && VISC ? Tr[NF] : T(0), TR && VISC ? Tr[TRW * NF + NF] : T(0));
+                                             1, out, TR ? trv(Tr, 0) : T(0), TR ? trv(Tr, TRW * NF) : T(0),
+                                             TR && VISC ? trv(Tr, NF) : T(0), TR && VISC ? trv(Tr, TRW * NF + NF) : T(0));
       T *z = Qb + cl * NQ + N * r;
 #pragma unroll
       for (int k = 0; k < N; ++k)
@@ -258,14 +315,14 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
 #pragma unroll
       for (int k = 0; k < N; ++k)
         U[k] = p[k * N];
-      const T *Tr = Tb + (cl * 6 + 2) * TRW * NF + r;
-      direction_pass<N, T, UNI, VISC, 1, TR>(A, tb, U, Nb[(cl * 6 + 2) * NF + r], Nb[(cl * 6 + 3) * NF + r],
-                                             VISC ? Nd[(cl * 6 + 2) * NF + r] : T(0),
-                                             VISC ? Nd[(cl * 6 + 3) * NF + r] : T(0), s_nbr[cl * 6 + 2] < 0,
+      const T *Tr = TR ? own_tr(cl, 2) + r : nullptr;
+      direction_pass<N, T, UNI, VISC, 1, TR>(A, tb, U, nbv(cl, 2, r), nbv(cl, 3, r),
+                                             nbd(cl, 2, r),
+                                             nbd(cl, 3, r), s_nbr[cl * 6 + 2] < 0,
                                              s_nbr[cl * 6 + 3] < 0, r, faces(cl, 2), faces(cl, 3),
-                                             geo(cl) + NQ + off, N, out, TR ? Tr[0] : T(0),
-                                             TR ? Tr[TRW * NF] : T(0), TR && VISC ? Tr[NF] : T(0),
-                                             TR && VISC ? Tr[TRW * NF + NF] : T(0));
+                                             geo(cl) + NQ + off, N, out, TR ? trv(Tr, 0) : T(0),
+                                             TR ? trv(Tr, TRW * NF) : T(0), TR && VISC ? trv(Tr, NF) : T(0),
+                                             TR && VISC ? trv(Tr, TRW * NF + NF) : T(0));
       T *z = Qb + cl * NQ + off;
 #pragma unroll
       for (int k = 0; k < N; ++k)
@@ -284,13 +341,13 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
       for (int k = 0; k < N; ++k)
         U[k] = p[k * NF];
       const T *G  = geo(cl);
-      const T *Tr = Tb + (cl * 6 + 4) * TRW * NF + r;
-      direction_pass<N, T, UNI, VISC, 2, TR>(A, tb, U, Nb[(cl * 6 + 4) * NF + r], Nb[(cl * 6 + 5) * NF + r],
-                                             VISC ? Nd[(cl * 6 + 4) * NF + r] : T(0),
-                                             VISC ? Nd[(cl * 6 + 5) * NF + r] : T(0), s_nbr[cl * 6 + 4] < 0,
+      const T *Tr = TR ? own_tr(cl, 4) + r : nullptr;
+      direction_pass<N, T, UNI, VISC, 2, TR>(A, tb, U, nbv(cl, 4, r), nbv(cl, 5, r),
+                                             nbd(cl, 4, r),
+                                             nbd(cl, 5, r), s_nbr[cl * 6 + 4] < 0,
                                              s_nbr[cl * 6 + 5] < 0, r, faces(cl, 4), faces(cl, 5), G + 2 * NQ + r,
-                                             NF, out, TR ? Tr[0] : T(0), TR ? Tr[TRW * NF] : T(0),
-                                             TR && VISC ? Tr[NF] : T(0), TR && VISC ? Tr[TRW * NF + NF] : T(0));
+                                             NF, out, TR ? trv(Tr, 0) : T(0), TR ? trv(Tr, TRW * NF) : T(0),
+                                             TR && VISC ? trv(Tr, NF) : T(0), TR && VISC ? trv(Tr, TRW * NF + NF) : T(0));
       T              *z  = Qb + cl * NQ + r;
       const long long gb = (cell0 + cl) * NQ + r;
       double          next[N]; // the next stage's input along the pencil (traces)
@@ -406,18 +463,49 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
     }
 }
 
+// resident CTAs per SM the compiler has to allow for: with traces at degree 4
+// on field geometry the FP64 kernel's shared memory admits 7 CTAs per SM, and
+// 72 registers (no spills) let all 7 reside; measured on GB300 on 64^3 curved
+// cells, 2.2 % faster than the unbounded 94 registers (5 CTAs)
+template <int N, typename T, bool UNI, bool VISC, bool TR>
+constexpr int gauss_min_blocks()
+{
+  return TR && !UNI && !VISC && N == 5 && sizeof(T) == sizeof(double) ? 7 : 1;
+}
+
 template <int N, typename T, bool UNI, bool VISC, bool TR, bool INC>
 __global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS) stage_gauss_kernel(const StageArgs A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   stage_gauss_cta<N, T, UNI, VISC, TR, INC>(A, A.cell_begin + (long long)blockIdx.x * StageShape<N, T, UNI, VISC>::C,
-                                       smem_raw);
+                                            smem_raw);
+}
+
+// the same with the resident-CTA bound (only where gauss_min_blocks > 1: an
+// explicit bound of 1 changes the register allocation of the others)
+template <int N, typename T, bool UNI, bool VISC, bool TR, bool INC>
+__global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS, (gauss_min_blocks<N, T, UNI, VISC, TR>()))
+  stage_gauss_kernel_bounded(const StageArgs A)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  stage_gauss_cta<N, T, UNI, VISC, TR, INC>(A, A.cell_begin + (long long)blockIdx.x * StageShape<N, T, UNI, VISC>::C,
+                                            smem_raw);
+}
+
+template <int N, typename T, bool UNI, bool VISC, bool TR, bool INC>
+constexpr auto gauss_kernel()
+{
+  if constexpr (gauss_min_blocks<N, T, UNI, VISC, TR>() > 1)
+    return stage_gauss_kernel_bounded<N, T, UNI, VISC, TR, INC>;
+  else
+    return stage_gauss_kernel<N, T, UNI, VISC, TR, INC>;
 }
 
 template <int N, typename T, bool UNI, bool VISC, bool TR, bool INC = false>
 cudaError_t launch_stage_gauss_t(const StageArgs &args, cudaStream_t stream)
 {
   using GS = GaussShape<N, T, UNI, VISC, TR>;
+  constexpr auto kernel = gauss_kernel<N, T, UNI, VISC, TR, INC>();
   static unsigned long long configured = 0;
   int                       dev        = 0;
   cudaError_t               e          = cudaGetDevice(&dev);
@@ -425,15 +513,14 @@ cudaError_t launch_stage_gauss_t(const StageArgs &args, cudaStream_t stream)
     return e;
   if (dev >= 64 || !((configured >> dev) & 1ull))
     {
-      e = cudaFuncSetAttribute(stage_gauss_kernel<N, T, UNI, VISC, TR, INC>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, GS::SMEM);
+      e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, GS::SMEM);
       if (e != cudaSuccess)
         return e;
       if (dev < 64)
         configured |= 1ull << dev;
     }
   const long long blocks = (args.n_cells - args.cell_begin + GS::C - 1) / GS::C;
-  stage_gauss_kernel<N, T, UNI, VISC, TR, INC><<<(unsigned)blocks, GS::THREADS, GS::SMEM, stream>>>(args);
+  kernel<<<(unsigned)blocks, GS::THREADS, GS::SMEM, stream>>>(args);
   return cudaGetLastError();
 }
 
