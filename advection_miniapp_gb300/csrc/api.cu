@@ -960,6 +960,13 @@ int increment_stage(adv_handle *h, const std::vector<double> &ai, const std::vec
   return ADV_OK;
 }
 
+// values per binary32 register of the increment form: n_dofs rounded up to 4,
+// so that every register starts on 16 bytes
+int64_t inc32_stride(const adv_handle &h)
+{
+  return (h.mesh.n_dofs + 3) / 4 * 4;
+}
+
 // FP32 increments in the collocation form, with the anchor's K0 folded out
 // of the FP64 registers.  Within a block, with C the sum of the b dt of the
 // stages since the anchor, the kernels carry e = u - u_a - C K0 (FP64) and
@@ -982,7 +989,7 @@ int increment_stage_folded(adv_handle *h, const std::vector<double> &ai, const s
   const int m      = h->cfg.anchor_interval > 0 ? h->cfg.anchor_interval : 4;
   const int j      = step % m;
   const int q      = j * ns + st; // stage index inside the block
-  const int64_t nd = h->mesh.n_dofs;
+  const int64_t nd = inc32_stride(*h);
   float    *G[2]   = {h->d_inc32, h->d_inc32 + nd}, *K32 = h->d_inc32 + 2 * nd;
   double   *K0     = h->d_scratch[1];
   prec             = q == 0 ? 0 : 1;
@@ -1030,8 +1037,8 @@ int ensure_inc32(adv_handle *h)
 {
   if (!h->d_inc32)
     {
-      ADV_CUDA(cudaMalloc(&h->d_inc32, 3 * h->mesh.n_dofs * sizeof(float)));
-      h->device_bytes += 3 * h->mesh.n_dofs * (int64_t)sizeof(float);
+      ADV_CUDA(cudaMalloc(&h->d_inc32, 3 * inc32_stride(*h) * sizeof(float)));
+      h->device_bytes += 3 * inc32_stride(*h) * (int64_t)sizeof(float);
     }
   return ADV_OK;
 }

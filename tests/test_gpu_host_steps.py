@@ -32,6 +32,11 @@ CASES = {
                         velocity_period=0.5, initial_condition=1, ic_params=(0.3, 0.5, 0.5, 0.1),
                         boundary_value=0),
     "sipg-k3": dict(degree=3, n_cells=(20, 20, 24), diffusion=1e-2),
+    # zero Dirichlet data, constant velocity: the FP32 increment form with boundary faces
+    "dirichlet-zero-k4": dict(degree=4, n_cells=(16, 16, 12), periodic=0, boundary_value=0, initial_condition=1,
+                              ic_params=(0.5, 0.5, 0.5, 0.15), mesh_type=1, deformation=0.05),
+    # an odd number of DoFs (105 cells of 125): registers and cells off 16 bytes
+    "odd-dofs-k4": dict(degree=4, n_cells=(5, 3, 7), mesh_type=1, deformation=0.05),
 }
 
 

@@ -39,6 +39,10 @@ CASES = {
                              velocity_period=0.5, diffusion=1e-2, penalty_factor=1.0, initial_condition=1,
                              ic_params=(0.3, 0.5, 0.5, 0.2), boundary_value=0),
     "sipg-periodic-k2": dict(degree=2, n_cells=(3, 3, 3), diffusion=3e-2),
+    # zero Dirichlet data with constant velocity: a linear, time-independent
+    # operator with boundary faces (the FP32 increment form applies)
+    "dirichlet-zero-k3": dict(degree=3, n_cells=(3, 3, 4), periodic=0, boundary_value=0, initial_condition=1,
+                              ic_params=(0.5, 0.5, 0.5, 0.15), mesh_type=1, deformation=0.05),
     "sipg-exact-bc-k5-skew": dict(degree=5, n_cells=(2, 2, 3), periodic=0, diffusion=1e-3, factor_skew=0.5,
                                   initial_condition=2, boundary_value=1),
 }
@@ -299,7 +303,7 @@ def test_fp32_increment_form_against_oracle(cuda, oracle_mod, adv_lib, case, for
 
 @pytest.mark.parametrize("form", [1, 2])
 @pytest.mark.parametrize("interval", [2, 4, 8])
-@pytest.mark.parametrize("case", ["curved-k4", "affine-k3", "sipg-periodic-k2"])
+@pytest.mark.parametrize("case", ["curved-k4", "affine-k3", "affine-k4", "dirichlet-zero-k3", "sipg-periodic-k2"])
 def test_fp32_increment_anchor_interval_against_oracle(cuda, oracle_mod, adv_lib, case, interval, form):
     """FP32 increments anchored every `interval` steps, 6 steps (a whole block
     and a partial one, or one partial block): the register rotation of the
