@@ -20,7 +20,7 @@ import torch
 from . import (FORM_AUTO, FORM_COLLOCATION, FORM_COLLOCATION_NO_TRACES, FORM_NODAL, AdvectionOperation, IC_BLOB, IC_SINE_GAUSS, IC_WAVE, LSRK_3_3, LSRK_5_4, LSRK_7_4, LSRK_9_5,
                LowStorageRungeKuttaIntegrator, MESH_CARTESIAN, MESH_DEFORMED, PRECISION_FP32_INCREMENT,
                PRECISION_FP32_OPERATOR,
-               PRECISION_FP64, make_config, workload_config)
+               PRECISION_FP64, VELOCITY_ROTATING, make_config, workload_config)
 
 SCHEMES = {"3_3": LSRK_3_3, "5_4": LSRK_5_4, "7_4": LSRK_7_4, "9_5": LSRK_9_5}
 ICS = {"sine-gauss": IC_SINE_GAUSS, "blob": IC_BLOB, "wave": IC_WAVE}
@@ -142,6 +142,7 @@ def main(argv=None):
     u = op.initialize_dof_vector()
     op.project_initial(u)
     r, k = op.initialize_dof_vector(), op.initialize_dof_vector()
+    u_start = u.clone() if cfg.velocity_type == VELOCITY_ROTATING else None
 
     n_out = [0]
 
@@ -182,6 +183,14 @@ def main(argv=None):
     res = {"workload": args.workload, "precision": args.precision, "n_dofs": op.n_dofs, "steps": args.steps,
            "dt": dt, "t_end": t, "rel_l2_error": rel, "mass_energy": list(me), "s_per_step": per_step,
            "gdofs_per_stage": stage_rate}
+    if u_start is not None:
+        # return to the start of the time-periodic rotating flow
+        # (advection_solver_variable.cc:1249-1252): small when t_end is a
+        # multiple of the period and there is no diffusion
+        ret = float((u - u_start).abs().max() / u_start.abs().max())
+        res["return_to_start_max_rel"] = ret
+        if not args.json:
+            print(f"   Return to start: ||u(T) - u(0)||_inf / ||u(0)||_inf = {ret:.4e}")
     if args.compare_fp64 and precision != PRECISION_FP64:
         cfg.precision = PRECISION_FP64
         op64 = AdvectionOperation(cfg)
