@@ -160,21 +160,17 @@ __device__ __forceinline__ void sweep_eo(const EvenOdd<T> &M, const T (&in)[N], 
 // DL adds the SIPG derivative lifts lwd0 dlo + lwd1 dhi the same way (by
 // the symmetry lwd1[q] = -lwd0[n-1-q]: lde[q] (dlo - dhi) + ldo[q] (dlo + dhi)
 // at q, lde[q] (dlo - dhi) - ldo[q] (dlo + dhi) at n-1-q).
+// The sweep from the even and odd parts e[i] = in[i] + in[n-1-i],
+// o[i] = in[i] - in[n-1-i] and the middle value in[n/2] (odd n).
 template <int N, typename T, bool DL = false>
-__device__ __forceinline__ void sweep_eo_anti_lift(const EvenOdd<T> &M, const T (&in)[N], T phlo, T phhi,
-                                                   const T *lwe, const T *lwo, T (&out)[N], T dlo = T(0),
-                                                   T dhi = T(0), const T *lde = nullptr, const T *ldo = nullptr)
+__device__ __forceinline__ void sweep_eo_anti_lift_parts(const EvenOdd<T> &M, const T (&e)[N / 2],
+                                                         const T (&o)[N / 2], T mid, T phlo, T phhi, const T *lwe,
+                                                         const T *lwo, T (&out)[N], T dlo = T(0), T dhi = T(0),
+                                                         const T *lde = nullptr, const T *ldo = nullptr)
 {
-  constexpr int H = N / 2;
-  T             e[H], o[H];
-#pragma unroll
-  for (int i = 0; i < H; ++i)
-    {
-      e[i] = in[i] + in[N - 1 - i];
-      o[i] = in[i] - in[N - 1 - i];
-    }
-  const T ps = phlo + phhi, pd = phlo - phhi;
-  const T ds = dlo - dhi, dd = dlo + dhi;
+  constexpr int H  = N / 2;
+  const T       ps = phlo + phhi, pd = phlo - phhi;
+  const T       ds = dlo - dhi, dd = dlo + dhi;
 #pragma unroll
   for (int q = 0; q < H; ++q)
     {
@@ -186,7 +182,7 @@ __device__ __forceinline__ void sweep_eo_anti_lift(const EvenOdd<T> &M, const T 
           O = fma(M.o[q][i], o[i], O);
         }
       if (N % 2)
-        E = fma(M.ce[q], in[H], E);
+        E = fma(M.ce[q], mid, E);
       T a = fma(lwe[q], ps, O);
       T b = fma(lwo[q], pd, E);
       if (DL)
@@ -208,6 +204,23 @@ __device__ __forceinline__ void sweep_eo_anti_lift(const EvenOdd<T> &M, const T 
         m = fma(lde[H], ds, m);
       out[H] = m;
     }
+}
+
+template <int N, typename T, bool DL = false>
+__device__ __forceinline__ void sweep_eo_anti_lift(const EvenOdd<T> &M, const T (&in)[N], T phlo, T phhi,
+                                                   const T *lwe, const T *lwo, T (&out)[N], T dlo = T(0),
+                                                   T dhi = T(0), const T *lde = nullptr, const T *ldo = nullptr)
+{
+  constexpr int H = N / 2;
+  T             e[H], o[H];
+#pragma unroll
+  for (int i = 0; i < H; ++i)
+    {
+      e[i] = in[i] + in[N - 1 - i];
+      o[i] = in[i] - in[N - 1 - i];
+    }
+  sweep_eo_anti_lift_parts<N, T, DL>(M, e, o, N % 2 ? in[H] : T(0), phlo, phhi, lwe, lwo, out, dlo, dhi, lde,
+                                     ldo);
 }
 
 // Sweep with the cheaper of the two forms: even-odd pays off from n = 5.
@@ -318,7 +331,25 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
       // or vt (field); the lifts ride on the even-odd recombination
       const T cvd = Consts<T>::cv(A, D);
       const T sk  = A.has_skew ? Consts<T>::skew(A) : T(0);
-      T       w[N], du[N];
+      if (!UNI && !A.has_skew && sizeof(T) == sizeof(double))
+        {
+          // field, conservative form: the even and odd parts of vt U as
+          // c_i U_i +- c_j U_j with one product and two FMAs per mirrored
+          // pair (instead of two products and two additions)
+          constexpr int H = N / 2;
+          T             e[H], o[H];
+#pragma unroll
+          for (int i = 0; i < H; ++i)
+            {
+              const T p = vt[(N - 1 - i) * vstride] * U[N - 1 - i];
+              e[i]      = fma(vt[i * vstride], U[i], p);
+              o[i]      = fma(vt[i * vstride], U[i], -p);
+            }
+          sweep_eo_anti_lift_parts<N, T>(tb.Dw_eo, e, o, N % 2 ? vt[H * vstride] * U[H] : T(0), phlo, phhi,
+                                         tb.lwe, tb.lwo, out);
+          return;
+        }
+      T w[N], du[N];
 #pragma unroll
       for (int q = 0; q < N; ++q)
         {

@@ -102,6 +102,11 @@ def fp_work_per_cell(n, curved=True, stage=True, collocation=False, traces=False
         flops = 3 * p * sf + 12 * n * sf
     own_i, own_f = (0, 0) if traces else (2 * n, 2 * (2 * n - 1))
     pass_i = own_i + 4 + n + di + 2 * n
+    if curved and n >= 5:
+        # FP64 on field geometry: the even and odd parts of vt U take one
+        # product and two FMAs per mirrored pair instead of two products and
+        # two additions (same flops)
+        pass_i -= n // 2
     pass_f = own_f + 6 + n + df + 4 * n
     inst += 3 * p * pass_i
     flops += 3 * p * pass_f
