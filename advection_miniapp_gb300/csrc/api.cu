@@ -979,11 +979,11 @@ int64_t inc32_stride(const adv_handle &h)
 // A stage reads 4 + 8 + 4 and writes 8 + 4 bytes per DoF instead of 24 + 16,
 // and issues one FP64 instruction per DoF instead of two.  The last stage of
 // a step inside a block writes the next step's start G = e' + (C + b) K0.
-// Buffers: u holds u_a, K0 a scratch vector, e lives in r; the two G
-// registers and K0 in binary32 share one allocation of 3 n_dofs floats.
+// Buffers: u holds u_a, K0 lives in k and e in r; the two G registers and K0
+// in binary32 share one allocation of 3 n_dofs floats.
 int increment_stage_folded(adv_handle *h, const std::vector<double> &ai, const std::vector<double> &bi, double t,
-                           double dt, int n_steps, int step, int st, double *u, double *r, adv::StageArgs &A,
-                           int &prec)
+                           double dt, int n_steps, int step, int st, double *u, double *r, double *k,
+                           adv::StageArgs &A, int &prec)
 {
   const int ns     = (int)bi.size();
   const int m      = h->cfg.anchor_interval > 0 ? h->cfg.anchor_interval : 4;
@@ -991,7 +991,7 @@ int increment_stage_folded(adv_handle *h, const std::vector<double> &ai, const s
   const int q      = j * ns + st; // stage index inside the block
   const int64_t nd = inc32_stride(*h);
   float    *G[2]   = {h->d_inc32, h->d_inc32 + nd}, *K32 = h->d_inc32 + 2 * nd;
-  double   *K0     = h->d_scratch[1];
+  double   *K0     = k;
   prec             = q == 0 ? 0 : 1;
   A                = base_args(*h, stage_time(ai, bi, t + step * dt, dt, st), prec);
   A.gauss          = true;
@@ -1271,10 +1271,6 @@ int lsrk_steps_impl(adv_handle *h, int scheme, double t, double dt, int n_steps,
     }
   if (increment_form_applies(*h))
     {
-      if (int e = ensure_scratch(h, 0))
-        return e;
-      if (int e = ensure_scratch(h, 1))
-        return e;
       const bool gauss = n_steps > 0 && h->cfg.fused_form != ADV_FORM_NODAL;
       if (gauss)
         {
@@ -1282,9 +1278,13 @@ int lsrk_steps_impl(adv_handle *h, int scheme, double t, double dt, int n_steps,
             return e;
           return run_steps(h, n_steps, ns, true, false, u, host, s,
                            [&](int step, int st, adv::StageArgs &A, int &prec) {
-                             return increment_stage_folded(h, ai, bi, t, dt, n_steps, step, st, u, r, A, prec);
+                             return increment_stage_folded(h, ai, bi, t, dt, n_steps, step, st, u, r, k, A, prec);
                            });
         }
+      if (int e = ensure_scratch(h, 0))
+        return e;
+      if (int e = ensure_scratch(h, 1))
+        return e;
       return run_steps(h, n_steps, ns, gauss, false, u, host, s,
                        [&](int step, int st, adv::StageArgs &A, int &prec) {
                          return increment_stage(h, ai, bi, t, dt, n_steps, step, st, gauss, u, r, k, A, prec);
