@@ -200,6 +200,18 @@ public:
           "perform_time_step");
   }
 
+  // n_steps steps on a solution in host memory (page-locked for the copies
+  // to overlap): copied in, advanced and copied back (adv_lsrk_steps_host);
+  // host_solution holds the result once the operator's stream has passed it.
+  void perform_time_steps_host(const AdvectionOperation &op, const double current_time, const double time_step,
+                               const int n_steps, double *host_solution, DeviceVector &solution,
+                               DeviceVector &vec_ri, DeviceVector &vec_ki) const
+  {
+    check(adv_lsrk_steps_host(op.handle(), scheme_, current_time, time_step, n_steps, host_solution,
+                              solution.data(), vec_ri.data(), vec_ki.data(), op.stream()),
+          "perform_time_steps_host");
+  }
+
   // Any other operator with the reference's perform_stage gets the
   // reference's stage loop (advection_solver.cc:906-939).
   template <typename VectorType, typename Operator>
