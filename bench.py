@@ -15,9 +15,10 @@ holds the FP32-operator path (FP64 vectors) with its L2 error next to the FP64
 one; `e2e` repeats the FP64 measurement through the C ABI's host-buffer entry
 point (adv_lsrk_steps_host), which copies the solution from pinned host memory
 to the device and back around every step; `roofline` and `cpu_baseline`
-explain the numbers.  With --gpus N > 1 (torchrun) every rank solves its own
-replica (the path has no data exchange between independent solves): weak
-scaling.
+explain the numbers; `serving` gives the p50/p99 solve latency of the
+serving loop on a 128-request mix beside one-at-a-time solving.  With
+--gpus N > 1 (torchrun) every rank solves its own replica (the path has no
+data exchange between independent solves): weak scaling.
 
 The reference arm (--impl reference) times the CPU oracle, the FP64 C++
 restatement of the reference's algorithm (the deal.II reference cannot be
@@ -50,6 +51,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-serving", action="store_true")
     return p.parse_args()
 
 
@@ -333,6 +335,24 @@ def e2e_fp64(torch, adv, args, stream):
     return dict(value=op.n_dofs * STAGES * args.steps / sec / 1e9, h2d=nb, d2h=nb)
 
 
+def serving_run(n_requests=128, rate=200.0):
+    """p50/p99 solve latency of the serving loop: the seeded request mix of
+    the serving workload (meshes of 4^3 to 32^3 cells, degrees 2-6, end
+    times 0.1-1, FP64 or FP32 operator), Poisson arrivals, shortest-first
+    admission of at most 16 solves at once, beside the same requests solved
+    one at a time in arrival order."""
+    from advection_miniapp_gb300 import serving as srv_mod
+    reqs = srv_mod.request_mix(n_requests, 0, rate)
+    _, srv, _ = srv_mod.run_mix(reqs, rate_clock=True, max_active=16, policy="shortest")
+    _, base = srv_mod.run_one_at_a_time(reqs, rate_clock=True)
+    keep = ("p50_latency_s", "p99_latency_s", "throughput_req_s", "gdof_stages_per_s", "wall_s")
+    server = {k: round(srv[k], 4) for k in keep}
+    server.update(failed=srv["failed"], max_rel_l2_error=srv["max_rel_l2_error"])
+    return {"requests": n_requests, "rate_req_s": rate, "admission": "shortest-first, 16 solves at once",
+            "latency": "arrival to completion", "server": server,
+            "one_at_a_time": {k: round(base[k], 4) for k in keep}}
+
+
 def ours(args):
     import torch
     import torch.distributed as dist
@@ -426,6 +446,10 @@ def ours(args):
         hbm_peak = json.load(open(peaks_file)).get("hbm_gbs", hbm_peak)
     inc_gbs = increment_bytes_per_dof_step(n) * n_dofs / (secinc / args.steps) / 1e9
 
+    serving = None
+    if not args.no_serving and world == 1:
+        serving = serving_run()
+
     cpu = None
     if not args.no_cpu_baseline:
         res = oracle_run(steps=10, warmup=0, time_budget=20.0)
@@ -490,6 +514,7 @@ def ours(args):
                                        "and 19 FP32 stages) over the block's time"},
             "clocks": rinc["clocks"]},
         "e2e": e2e,
+        "serving": serving,
         "gpu_launches": r64["launches"] + r32["launches"] + rinc["launches"],
         "clocks": r64["clocks"],
         "cpu_baseline": cpu,
