@@ -80,9 +80,10 @@ def test_host_steps_equal_device_steps(cuda, adv_lib, case, precision):
 
 @pytest.mark.parametrize("form", [1, 2, 3])
 @pytest.mark.parametrize("n_steps", [1, 3])
-def test_host_steps_every_form(cuda, adv_lib, form, n_steps):
+@pytest.mark.parametrize("precision", [0, 2])
+def test_host_steps_every_form(cuda, adv_lib, form, n_steps, precision):
     torch, adv = cuda, adv_lib
-    ref, out, dev = _run_both(torch, adv, CASES["deformed-k4-24"], 0, n_steps, adv.LSRK_3_3, form=form)
+    ref, out, dev = _run_both(torch, adv, CASES["deformed-k4-24"], precision, n_steps, adv.LSRK_3_3, form=form)
     assert np.array_equal(out, ref) and np.array_equal(dev, ref)
 
 
