@@ -1074,8 +1074,17 @@ HostChunks plan_chunks(const adv::Mesh &m)
   c.cell_dofs         = (int64_t)m.n * m.n * m.n;
   const int64_t bytes = m.n_dofs * (int64_t)sizeof(double);
   int           k     = (int)std::min<int64_t>(std::min(nz, 8), std::max<int64_t>(1, bytes / (2 << 20)));
-  for (int i = 0; i <= k; ++i)
-    c.z.push_back((int)((int64_t)nz * i / k));
+  // the last chunk is small (1/32 of the layers): its basis change after the
+  // end of the copies in and its copy out after the end of the last stage are
+  // the parts the pipeline cannot hide
+  const int tail = k > 1 ? std::max(1, nz / 32) : 0;
+  const int big  = tail ? k - 1 : k; // chunks before the tail
+  for (int i = 0; i < big; ++i)
+    c.z.push_back((int)((int64_t)(nz - tail) * i / big));
+  if (tail)
+    c.z.push_back(nz - tail);
+  c.z.push_back(nz);
+  c.z.erase(std::unique(c.z.begin(), c.z.end()), c.z.end()); // no empty chunk
   return c;
 }
 
@@ -1138,13 +1147,14 @@ int run_steps(adv_handle *h, int n_steps, int ns, bool gauss, bool traces, doubl
   };
   if (host)
     {
-      // copy in: chunk c on copy stream 0 after the work already on s; on a
-      // periodic mesh the top chunk goes first, so that the bottom chunk's
-      // first stage does not wait for the end of the copies
+      // copy in: chunk c on copy stream 0 after the work already on s; with
+      // the first stage run chunk by chunk (nodal form) on a periodic mesh the
+      // top chunk goes first, so that the bottom chunk's first stage does not
+      // wait for the end of the copies
       const int         nz   = h->mesh.nc[2];
       const bool        wrap = h->mesh.periodic;
       std::vector<int>  order;
-      if (wrap && nch > 2)
+      if (wrap && nch > 2 && !gauss)
         order.push_back(nch - 1);
       for (int c = 0; (int)order.size() < nch; ++c)
         order.push_back(c);
