@@ -981,9 +981,18 @@ int64_t inc32_stride(const adv_handle &h)
 // a step inside a block writes the next step's start G = e' + (C + b) K0.
 // Buffers: u holds u_a, K0 lives in k and e in r; the two G registers and K0
 // in binary32 share one allocation of 3 n_dofs floats.
+// The anchor reads the face traces of u_a (field geometry without SIPG): the
+// change of basis writes them for the first block, a traces-only launch for
+// the later blocks of the call (750 FP64 FMAs per cell against the 1,500 the
+// anchor saves; it writes no traces itself, another 750).
+bool anchor_traces(const adv_handle &h)
+{
+  return !h.mesh.uniform && h.cfg.diffusion == 0.0;
+}
+
 int increment_stage_folded(adv_handle *h, const std::vector<double> &ai, const std::vector<double> &bi, double t,
                            double dt, int n_steps, int step, int st, double *u, double *r, double *k,
-                           adv::StageArgs &A, int &prec)
+                           adv::StageArgs &A, int &prec, cudaStream_t s)
 {
   const int ns     = (int)bi.size();
   const int m      = h->cfg.anchor_interval > 0 ? h->cfg.anchor_interval : 4;
@@ -1002,6 +1011,16 @@ int increment_stage_folded(adv_handle *h, const std::vector<double> &ai, const s
       A.r_in  = u;
       A.a     = ai[0] * dt * A.out_scale;
       A.k_out = K0, A.k_out32 = K32, A.r_out32 = G[0];
+      if (anchor_traces(*h))
+        {
+          double *tr = static_cast<double *>(h->d_traces[0]);
+          if (step > 0)
+            {
+              ADV_CUDA(adv::launch_face_traces(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, s, tr, 1));
+              ++h->launches;
+            }
+          A.tr_in = tr;
+        }
       return ADV_OK;
     }
   // C: the b dt of the stages since the anchor, summed in stage order
@@ -1286,9 +1305,14 @@ int lsrk_steps_impl(adv_handle *h, int scheme, double t, double dt, int n_steps,
         {
           if (int e = ensure_inc32(h))
             return e;
-          return run_steps(h, n_steps, ns, true, false, u, host, s,
+          const bool tr = anchor_traces(*h);
+          if (tr)
+            if (int e = ensure_traces(h))
+              return e;
+          return run_steps(h, n_steps, ns, true, tr, u, host, s,
                            [&](int step, int st, adv::StageArgs &A, int &prec) {
-                             return increment_stage_folded(h, ai, bi, t, dt, n_steps, step, st, u, r, k, A, prec);
+                             return increment_stage_folded(h, ai, bi, t, dt, n_steps, step, st, u, r, k, A, prec,
+                                                           s);
                            });
         }
       if (int e = ensure_scratch(h, 0))

@@ -106,6 +106,11 @@ cudaError_t upload_tables_gauss32(const DevTables<double> *d, const DevTables<fl
 // (width 2: values and reference normal derivatives, for SIPG).
 cudaError_t launch_basis_change(int n, double *u, long long cell_begin, long long cell_end, bool to_gauss,
                                 cudaStream_t stream, double *traces = nullptr, int width = 1);
+// Face traces [6][width][n^2] per cell of the Gauss-point values in u (the
+// values at the face points, with width 2 also the reference normal
+// derivatives), for the cells [cell_begin, cell_end); u is not changed.
+cudaError_t launch_face_traces(int n, const double *u, long long cell_begin, long long cell_end,
+                               cudaStream_t stream, double *traces, int width);
 // cells processed per CTA by the stage kernel (for launch accounting)
 int stage_cells_per_block(int n, int precision);
 

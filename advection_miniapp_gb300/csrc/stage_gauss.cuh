@@ -410,7 +410,7 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
               next[k]     = 0.0;
             }
         }
-      if (TR)
+      if (TR && A.tr_out)
         {
           // the next input in the operator's precision (what the next stage
           // would load); z traces from registers, and the pencil goes to this
@@ -435,7 +435,7 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
             z[k * NF] = nt[k];
         }
     }
-  if (TR)
+  if (TR && A.tr_out)
     {
       __syncthreads();
       for (int w = tid; w < 2 * ncell * NF; w += NT)
@@ -530,9 +530,15 @@ cudaError_t launch_stage_gauss_n(const StageArgs &args, cudaStream_t stream)
   // face traces: FP64 only (the library's choice; the kernel code is generic)
   if constexpr (sizeof(T) == sizeof(double))
     if (args.tr_in)
-      return args.visc ? launch_stage_gauss_t<N, T, false, true, true>(args, stream)
-           : args.uniform ? launch_stage_gauss_t<N, T, true, false, true>(args, stream)
-                          : launch_stage_gauss_t<N, T, false, false, true>(args, stream);
+      {
+        // the FP32-increment anchor reads traces on field geometry without
+        // SIPG (and writes none)
+        if (args.inc32 && !args.visc && !args.uniform)
+          return launch_stage_gauss_t<N, T, false, false, true, true>(args, stream);
+        return args.visc ? launch_stage_gauss_t<N, T, false, true, true>(args, stream)
+             : args.uniform ? launch_stage_gauss_t<N, T, true, false, true>(args, stream)
+                            : launch_stage_gauss_t<N, T, false, false, true>(args, stream);
+      }
   if (args.inc32)
     return args.visc ? launch_stage_gauss_t<N, T, false, true, false, true>(args, stream)
          : args.uniform ? launch_stage_gauss_t<N, T, true, false, false, true>(args, stream)

@@ -7,8 +7,10 @@ namespace adv
 namespace
 {
 // u <- (M x M x M) u per cell, M = S (to the Gauss points) or S^-1, through
-// shared memory: one thread per pencil, C cells per CTA
-template <int N, bool TO_GAUSS>
+// shared memory: one thread per pencil, C cells per CTA.  MODE 1: to the
+// Gauss points (optionally with the face traces of the result), 0: back to
+// the Gauss-Lobatto nodes, 2: only the face traces of u (no change of basis).
+template <int N, int MODE>
 __global__ void __launch_bounds__(StageShape<N, double, true, false>::THREADS)
   basis_kernel(double *u, long long cell_begin, long long cell_end, double *traces, int width)
 {
@@ -23,11 +25,12 @@ __global__ void __launch_bounds__(StageShape<N, double, true, false>::THREADS)
   const int                ncell = (int)min((long long)C, cell_end - cell0);
   const int                tid   = threadIdx.x;
   double                  *g     = u + cell0 * NQ;
+  constexpr bool TO_GAUSS = MODE == 1;
   for (int i = tid; i < ncell * NQ; i += NT)
     buf[i] = g[i];
   __syncthreads();
 #pragma unroll
-  for (int d = 0; d < 3; ++d)
+  for (int d = 0; d < (MODE == 2 ? 0 : 3); ++d)
     {
       for (int w = tid; w < ncell * NF; w += NT)
         {
@@ -49,9 +52,10 @@ __global__ void __launch_bounds__(StageShape<N, double, true, false>::THREADS)
         }
       __syncthreads();
     }
-  for (int i = tid; i < ncell * NQ; i += NT)
-    g[i] = buf[i];
-  if (TO_GAUSS && traces)
+  if (MODE != 2)
+    for (int i = tid; i < ncell * NQ; i += NT)
+      g[i] = buf[i];
+  if (MODE != 0 && traces)
     {
       // face traces of the result, [6][width][NF] per cell (StageArgs::tr_in):
       // values, and with width 2 also reference normal derivatives
@@ -80,17 +84,19 @@ __global__ void __launch_bounds__(StageShape<N, double, true, false>::THREADS)
 }
 
 template <int N>
-cudaError_t launch_basis_n(double *u, long long cell_begin, long long cell_end, bool to_gauss, cudaStream_t s,
+cudaError_t launch_basis_n(double *u, long long cell_begin, long long cell_end, int mode, cudaStream_t s,
                            double *traces, int width)
 {
   using SH               = StageShape<N, double, true, false>;
   const long long blocks = (cell_end - cell_begin + SH::C - 1) / SH::C;
   if (blocks <= 0)
     return cudaSuccess;
-  if (to_gauss)
-    basis_kernel<N, true><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, traces, width);
+  if (mode == 1)
+    basis_kernel<N, 1><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, traces, width);
+  else if (mode == 2)
+    basis_kernel<N, 2><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, traces, width);
   else
-    basis_kernel<N, false><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, nullptr, 1);
+    basis_kernel<N, 0><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, nullptr, 1);
   return cudaGetLastError();
 }
 } // namespace
@@ -105,18 +111,33 @@ cudaError_t launch_stage_gauss_fp64(int n, const StageArgs &args, cudaStream_t s
   return launch_stage_gauss_any<double>(n, args, stream);
 }
 
-cudaError_t launch_basis_change(int n, double *u, long long cell_begin, long long cell_end, bool to_gauss,
-                                cudaStream_t stream, double *traces, int width)
+namespace
+{
+cudaError_t launch_basis_mode(int n, double *u, long long cell_begin, long long cell_end, int mode,
+                              cudaStream_t stream, double *traces, int width)
 {
   switch (n)
     {
-      case 2: return launch_basis_n<2>(u, cell_begin, cell_end, to_gauss, stream, traces, width);
-      case 3: return launch_basis_n<3>(u, cell_begin, cell_end, to_gauss, stream, traces, width);
-      case 4: return launch_basis_n<4>(u, cell_begin, cell_end, to_gauss, stream, traces, width);
-      case 5: return launch_basis_n<5>(u, cell_begin, cell_end, to_gauss, stream, traces, width);
-      case 6: return launch_basis_n<6>(u, cell_begin, cell_end, to_gauss, stream, traces, width);
-      case 7: return launch_basis_n<7>(u, cell_begin, cell_end, to_gauss, stream, traces, width);
+      case 2: return launch_basis_n<2>(u, cell_begin, cell_end, mode, stream, traces, width);
+      case 3: return launch_basis_n<3>(u, cell_begin, cell_end, mode, stream, traces, width);
+      case 4: return launch_basis_n<4>(u, cell_begin, cell_end, mode, stream, traces, width);
+      case 5: return launch_basis_n<5>(u, cell_begin, cell_end, mode, stream, traces, width);
+      case 6: return launch_basis_n<6>(u, cell_begin, cell_end, mode, stream, traces, width);
+      case 7: return launch_basis_n<7>(u, cell_begin, cell_end, mode, stream, traces, width);
       default: return cudaErrorInvalidValue;
     }
+}
+} // namespace
+
+cudaError_t launch_basis_change(int n, double *u, long long cell_begin, long long cell_end, bool to_gauss,
+                                cudaStream_t stream, double *traces, int width)
+{
+  return launch_basis_mode(n, u, cell_begin, cell_end, to_gauss ? 1 : 0, stream, traces, width);
+}
+
+cudaError_t launch_face_traces(int n, const double *u, long long cell_begin, long long cell_end,
+                               cudaStream_t stream, double *traces, int width)
+{
+  return launch_basis_mode(n, const_cast<double *>(u), cell_begin, cell_end, 2, stream, traces, width);
 }
 } // namespace adv
