@@ -87,6 +87,26 @@ def test_host_steps_every_form(cuda, adv_lib, form, n_steps, precision):
     assert np.array_equal(out, ref) and np.array_equal(dev, ref)
 
 
+def test_host_steps_pageable_host_memory(cuda, adv_lib):
+    """Host memory that is not page-locked: the copies cannot overlap, the
+    results are the same."""
+    torch, adv = cuda, adv_lib
+    op = adv.AdvectionOperation(**CASES["deformed-k4-24"])
+    dt = op.time_step(0.5)
+    u0 = op.initialize_dof_vector()
+    op.project_initial(u0)
+    u, r, k = u0.clone(), op.initialize_dof_vector(), op.initialize_dof_vector()
+    op.lsrk_steps(adv.LSRK_5_4, 0.0, dt, 2, u, r, k)
+    host = u0.cpu().clone()
+    assert not host.is_pinned()
+    ud, rd, kd = op.initialize_dof_vector(), op.initialize_dof_vector(), op.initialize_dof_vector()
+    torch.cuda.synchronize()
+    op.lsrk_steps_host(adv.LSRK_5_4, 0.0, dt, 2, host, ud, rd, kd)
+    torch.cuda.synchronize()
+    assert np.array_equal(host.numpy(), u.cpu().numpy())
+    op.close()
+
+
 def test_host_steps_zero_steps_copies_in(cuda, adv_lib):
     torch, adv = cuda, adv_lib
     op = adv.AdvectionOperation(**CASES["small-k2"])
