@@ -59,15 +59,16 @@ struct GaussShape
     (2 * C * N * N * N + NB_VALUES);
   // field geometry with traces: the face coefficients are read from global
   // memory in the direction passes (one read per face point) instead of being
-  // staged, which frees 12 C n^2 values of shared memory per CTA (one more
-  // resident CTA per SM at degree 4)
-  // SIPG: the cell geometry and face coefficients are read from global
-  // memory too; staged they would take 4 C n^3 + 12 C n^2 values (at degree 5
-  // in FP64, 72 KB of a 145 KB CTA, one CTA per SM).  Measured on GB300: the
-  // degree-5 SIPG workload gains 15 % (FP64) and 19 % (FP32); the advection
-  // kernels lose 7 % (FP64) and 4 % (FP32) with global geometry, so they keep
-  // staging it.
-  static constexpr bool GEO_GLOBAL   = VISC;
+  // staged, which frees 12 C n^2 values of shared memory per CTA.
+  // Cell geometry [vt0|vt1|vt2|idet] read from global memory in the passes
+  // (one read per point and direction) instead of staged by cp.async:
+  // with SIPG (staged it would take 4 C n^3 + 12 C n^2 values, at degree 5 in
+  // FP64 72 KB of a 145 KB CTA: +15 % FP64, +19 % FP32) and in the FP64
+  // kernel with traces (the CTA starts its passes without waiting for 20 KB
+  // of geometry: +3.6 % on 64^3 curved cells of degree 4 at 7 CTAs per SM).
+  // The other advection kernels keep staging it (measured 7 % / 4 % slower
+  // without).
+  static constexpr bool GEO_GLOBAL   = VISC || (TR && !UNI && sizeof(T) == sizeof(double));
   static constexpr bool FACES_GLOBAL = !UNI && (TR || VISC || sizeof(T) == sizeof(float));
   static constexpr int  FB_VALUES    = UNI || FACES_GLOBAL ? 0 : 12 * C * N * N;
   static constexpr int  GB_VALUES    = UNI || GEO_GLOBAL ? 0 : 4 * C * N * N * N;
@@ -464,9 +465,10 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
 }
 
 // resident CTAs per SM the compiler has to allow for: with traces at degree 4
-// on field geometry the FP64 kernel's shared memory admits 7 CTAs per SM, and
-// 72 registers (no spills) let all 7 reside; measured on GB300 on 64^3 curved
-// cells, 2.2 % faster than the unbounded 94 registers (5 CTAs)
+// on field geometry the FP64 kernel is bounded to 72 registers (no spills),
+// 7 CTAs per SM; measured on GB300 on 64^3 curved cells: faster than the
+// unbounded 94 registers (5 CTAs, 2.2 %) and than 8 or 9 CTAs (64 and 56
+// registers with spills)
 template <int N, typename T, bool UNI, bool VISC, bool TR>
 constexpr int gauss_min_blocks()
 {
