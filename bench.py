@@ -103,15 +103,18 @@ def fp_work_per_cell(n, curved=True, stage=True, collocation=False, traces=False
         inst = 3 * p * si + 12 * n * si
         flops = 3 * p * sf + 12 * n * sf
     own_i, own_f = (0, 0) if traces else (2 * n, 2 * (2 * n - 1))
-    pass_i = own_i + 4 + n + di + 2 * n
+    # per pencil and direction: 4 for the two face fluxes and 2 for their
+    # sum and difference, n products vt U, the lifted even-odd sweep, n lift
+    # FMAs and n additions into the accumulated Z (not in the first direction)
+    pass_i = own_i + 4 + 2 + n + di + 2 * n
     if curved and n >= 5:
         # FP64 on field geometry: the even and odd parts of vt U take one
         # product and two FMAs per mirrored pair instead of two products and
         # two additions (same flops)
         pass_i -= n // 2
-    pass_f = own_f + 6 + n + df + 4 * n
-    inst += 3 * p * pass_i
-    flops += 3 * p * pass_f
+    pass_f = own_f + 6 + 2 + n + df + 4 * n
+    inst += 3 * p * pass_i - p * n
+    flops += 3 * p * pass_f - p * n
     if curved:
         inst += n ** 3
         flops += n ** 3
