@@ -1,6 +1,6 @@
 """Benchmark: GDoF/s per LSRK stage of the matrix-free DG advection operator.
 
-Workload (BASELINE configuration "plain method at GPU scale"): 64^3 cells of
+Workload (the plain method at GPU scale): 64^3 cells of
 the sine-deformed unit cube (amplitude 0.08), FE_DGQ degree 4 (125 DoFs per
 cell, 32,768,000 DoFs), velocity (1, 0.15, -0.05), periodic, upwind flux,
 LSRK(5,4), Courant 0.5 / k^1.5, seeded analytic initial data.  One "step" is
