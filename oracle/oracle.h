@@ -3,8 +3,8 @@
  *
  * This library restates, in plain FP64 C++ on the host, the algorithm of the
  * reference miniapp (kronbichler/advection_miniapp, advection_solver.cc and
- * its variants).  It is the checker for the CUDA implementation in the
- * advection_miniapp_gb300 package and the timed CPU baseline.  Only the
+ * its variants).  The tests compare the CUDA implementation in the
+ * advection_miniapp_gb300 package with it, and it is the timed CPU baseline.  Only the
  * tests, the smoke check and the CPU-baseline leg of the benchmark may load
  * it; the product never links or calls it.
  *
