@@ -1,7 +1,7 @@
 // CPU oracle for the matrix-free DG advection operator: TEST INFRASTRUCTURE.
 //
-// A plain FP64 restatement of the reference miniapp's algorithm, used as the
-// checker of the CUDA path and as the timed CPU baseline.  Each function
+// A plain FP64 restatement of the reference miniapp's algorithm: the tests
+// compare the CUDA path with it, and it is the timed CPU baseline.  Each function
 // names the reference lines (kronbichler/advection_miniapp) it follows.  The
 // arithmetic the reference delegates to deal.II (FEEvaluation,
 // FEFaceEvaluation, CellwiseInverseMassMatrix, MatrixFree::loop; deal.II >=
