@@ -160,7 +160,12 @@ __host__ __device__ __forceinline__ double exact_value(const ExactParams &e, dou
           s[d]           = y - floor(y);
           r2 += (s[d] - 0.5) * (s[d] - 0.5);
         }
+#ifdef __CUDA_ARCH__
+      // sin(2 pi s) as sinpi(2 s): exact argument reduction, no product with pi
+      return sinpi(2.0 * s[0]) * sinpi(2.0 * s[1]) * sinpi(2.0 * s[2]) + exp(-50.0 * r2);
+#else
       return sin(2.0 * kPi * s[0]) * sin(2.0 * kPi * s[1]) * sin(2.0 * kPi * s[2]) + exp(-50.0 * r2);
+#endif
     }
   if (e.type == ADV_IC_BLOB)
     {
@@ -172,9 +177,15 @@ __host__ __device__ __forceinline__ double exact_value(const ExactParams &e, dou
         }
       return exp(-r2 / (e.p[3] * e.p[3]));
     }
+#ifdef __CUDA_ARCH__
+  double r = sinpi(4.0 * (x[0] - tt * e.velocity[0]));
+  r *= cospi(4.0 * (x[1] - tt * e.velocity[1]));
+  r *= cospi(4.0 * (x[2] - tt * e.velocity[2]));
+#else
   double r = sin(4.0 * kPi * (x[0] - tt * e.velocity[0]));
   r *= cos(4.0 * kPi * (x[1] - tt * e.velocity[1]));
   r *= cos(4.0 * kPi * (x[2] - tt * e.velocity[2]));
+#endif
   return r;
 }
 
@@ -182,11 +193,10 @@ __host__ __device__ __forceinline__ double exact_value(const ExactParams &e, dou
 __device__ __forceinline__ void deform_dev(double A, const double lo[3], const double L[3],
                                            const double x[3], double y[3])
 {
-  const double kPi = 3.14159265358979323846;
-  double       s[3];
+  double s[3];
   for (int d = 0; d < 3; ++d)
     s[d] = (x[d] - lo[d]) / L[d];
   for (int d = 0; d < 3; ++d)
-    y[d] = x[d] + A * L[d] * sin(2.0 * kPi * s[(d + 1) % 3]) * sin(2.0 * kPi * s[(d + 2) % 3]);
+    y[d] = x[d] + A * L[d] * sinpi(2.0 * s[(d + 1) % 3]) * sinpi(2.0 * s[(d + 2) % 3]);
 }
 } // namespace adv

@@ -82,13 +82,12 @@ __device__ void tsweep_n(const double *const (&As)[K], const double *const (&ins
 // (the same arithmetic as deform_dev)
 __device__ void support_points(const DiagArgs &g, const double lo[3], double *X, double *sn)
 {
-  const double kPi = 3.14159265358979323846;
-  const int    n = g.n, nq = n * n * n;
+  const int n = g.n, nq = n * n * n;
   for (int i = threadIdx.x; i < 3 * n; i += blockDim.x)
     {
       const int    d = i / n, a = i % n;
       const double x = lo[d] + g.h[d] * g.gl[a];
-      sn[i]          = sin(2.0 * kPi * ((x - g.lo[d]) / g.L[d]));
+      sn[i]          = sinpi(2.0 * ((x - g.lo[d]) / g.L[d]));
     }
   __syncthreads();
   for (int i = threadIdx.x; i < nq; i += blockDim.x)
