@@ -87,6 +87,16 @@ def test_host_steps_every_form(cuda, adv_lib, form, n_steps, precision):
     assert np.array_equal(out, ref) and np.array_equal(dev, ref)
 
 
+@pytest.mark.parametrize("interval", [1, 2, 3])
+def test_host_steps_increment_blocks(cuda, adv_lib, interval):
+    """FP32 increments over several anchor blocks (face traces of each later
+    anchor from a traces-only launch) through the host path."""
+    torch, adv = cuda, adv_lib
+    cfg = dict(CASES["deformed-k4-24"], anchor_interval=interval)
+    ref, out, dev = _run_both(torch, adv, cfg, 2, 7, adv.LSRK_5_4)
+    assert np.array_equal(out, ref) and np.array_equal(dev, ref)
+
+
 def test_host_steps_pageable_host_memory(cuda, adv_lib):
     """Host memory that is not page-locked: the copies cannot overlap, the
     results are the same."""
