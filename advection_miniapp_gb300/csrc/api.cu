@@ -439,6 +439,34 @@ int check_device(const adv_handle *h)
 }
 } // namespace
 
+// ---------------------------------------------------------------------------
+// Static stage scratch of adv_perform_stage_noalloc.  Callers that cannot
+// allocate device memory mid-solve (memory-budgeted serving, latency-critical
+// loops, memory owned by another allocator) get the staging buffer for an
+// output that aliases r_in from this file-scope array instead of a
+// handle-owned vector.  In host code the array's name is a host-side shadow,
+// not a device address: create_handle looks the device address up with the
+// handle's device current and keeps it in the handle.  That lookup also
+// loads this translation unit's module on the device (CUDA loads modules
+// lazily), so the array's memory is committed when a handle is created and
+// never inside a stage call; a handle lives no longer than the context its
+// own buffers belong to, so its copy of the address cannot go stale.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) double g_noalloc_stage_scratch[ADV_NOALLOC_MAX_DOFS];
+
+namespace
+{
+int lookup_noalloc_scratch(double **out)
+{
+  void       *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_stage_scratch);
+  if (e != cudaSuccess)
+    return cuda_fail(e, "cudaGetSymbolAddress of the static stage scratch");
+  *out = static_cast<double *>(p);
+  return ADV_OK;
+}
+} // namespace
+
 namespace adv
 {
 namespace detail
@@ -534,6 +562,8 @@ int create_handle(const adv_config *cfg, int z_begin, int z_end, adv_handle **ou
           break;
         }
       if ((rc = ensure_tables(h->device)))
+        break;
+      if ((rc = lookup_noalloc_scratch(&h->noalloc_scratch)))
         break;
       if (z_end >= 0)
         adv::setup_slab(h->cfg, z_begin, z_end, h->mesh);
@@ -1534,46 +1564,14 @@ int adv_measure_fma_peak(int precision, double *tflops, void *stream)
 
 } // extern "C"
 
-// ---------------------------------------------------------------------------
-// Allocation-free stage (adv_perform_stage_noalloc).  Callers that cannot
-// allocate device memory mid-solve (memory-budgeted serving, latency-critical
-// loops, memory owned by another allocator) get the staging buffer for an
-// output that aliases r_in from this file-scope array instead of a
-// handle-owned vector.  Host code must not take the array's address
-// directly (in host code the name is a host-side shadow, not a device
-// address): noalloc_scratch() looks up the device address once per device
-// with that device current.
-// ---------------------------------------------------------------------------
-static __device__ __align__(256) double g_noalloc_stage_scratch[ADV_NOALLOC_MAX_DOFS];
-
-namespace
-{
-std::mutex g_noalloc_mutex;
-double    *g_noalloc_ptr[256] = {};
-
-int noalloc_scratch(int device, double **out)
-{
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (device < 0 || device >= 256)
-    return fail(ADV_ERR_INVALID, "device index out of range");
-  if (!g_noalloc_ptr[device])
-    {
-      void       *p = nullptr;
-      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_stage_scratch);
-      if (e != cudaSuccess)
-        return cuda_fail(e, "cudaGetSymbolAddress of the static stage scratch");
-      g_noalloc_ptr[device] = static_cast<double *>(p);
-    }
-  *out = g_noalloc_ptr[device];
-  return ADV_OK;
-}
-} // namespace
-
 extern "C" int adv_perform_stage_noalloc(adv_handle *h, double t, double b_dt, double a_dt,
                                          const double *r_in, double *k, double *u, double *r_out,
                                          void *stream)
 {
   (void)k; // scratch in the reference's semantics; this variant does not need it
+  // NVTX range and optional call timing like every other entry point (event
+  // records, no device memory)
+  adv::detail::CallTrace trace_(h, "adv_perform_stage_noalloc", (cudaStream_t)stream);
   if (!h || !r_in || !u || (a_dt != 0.0 && !r_out))
     return fail(ADV_ERR_INVALID, "null argument");
   if (a_dt != 0.0 && r_out == u)
@@ -1585,9 +1583,9 @@ extern "C" int adv_perform_stage_noalloc(adv_handle *h, double t, double b_dt, d
                                    "; use adv_perform_stage");
   if (int e = check_device(h))
     return e;
-  double *scratch = nullptr;
-  if (int e = noalloc_scratch(h->device, &scratch))
-    return e;
+  double *scratch = h->noalloc_scratch;
+  if (!scratch)
+    return fail(ADV_ERR_INVALID, "handle has no static stage scratch address");
   cudaStream_t   s   = (cudaStream_t)stream;
   const size_t   nb  = h->mesh.n_dofs * sizeof(double);
   adv::StageArgs A   = base_args(*h, t);

@@ -32,6 +32,9 @@ struct adv_handle
   double  *d_scratch[2]  = {};
   void    *d_traces[2]   = {}; // face traces of the collocation step loop (lazily allocated)
   float   *d_inc32       = nullptr; // FP32 increments: two G registers and K0 in binary32 (lazily)
+  // device address of the library's static stage scratch (adv_perform_stage_noalloc),
+  // looked up when the handle is created, with its device current
+  double  *noalloc_scratch = nullptr;
   int64_t  device_bytes  = 0;
   int64_t  launches      = 0;
   adv::DiagArgs diag;

@@ -327,16 +327,18 @@ int adv_measure_fma_peak(int precision, double *tflops, void *stream);
  * whose device memory is owned by another allocator.  adv_perform_stage
  * stages an output that aliases r_in in a handle-owned vector it allocates
  * on first use; this variant stages it in a file-scope device array of
- * ADV_NOALLOC_MAX_DOFS doubles (16 MiB, held by every GPU that loads the
- * library until the process exits) and calls no allocating routine.
- * Meshes with more than ADV_NOALLOC_MAX_DOFS DoFs are rejected with
- * ADV_ERR_INVALID.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture.  All calls share the one array: calls
- * whose kernels overlap on the GPU (different streams, or different
- * handles) race on it.  Nothing in it needs to start at zero: each call
- * overwrites every staged value before copying it out.  Same arguments,
- * aliasing rules and results as adv_perform_stage; `k` is not touched. */
+ * ADV_NOALLOC_MAX_DOFS doubles (16 MiB) and calls no allocating routine.
+ * adv_create (and adv_create_slab) looks up the array's device address
+ * (cudaGetSymbolAddress) with the handle's device current and keeps it in
+ * the handle; the lookup loads the library module that holds the array, so
+ * its 16 MiB are committed on that device when the first handle is created
+ * there, and stay until the process exits.  Meshes with more than
+ * ADV_NOALLOC_MAX_DOFS DoFs are rejected with ADV_ERR_INVALID.  All calls
+ * share the one array: calls whose kernels overlap on the GPU (different
+ * streams, or different handles) race on it.  Nothing in it needs to start
+ * at zero: each call overwrites every staged value before copying it out.
+ * Same arguments, aliasing rules and results as adv_perform_stage; `k` is
+ * not touched.  Traced and timed like the other entry points. */
 #define ADV_NOALLOC_MAX_DOFS (1 << 21)
 int adv_perform_stage_noalloc(adv_handle *h, double t, double b_dt, double a_dt, const double *r_in,
                               double *k, double *u, double *r_out, void *stream);

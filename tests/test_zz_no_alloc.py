@@ -71,14 +71,19 @@ def test_noalloc_stage_matches_perform_stage(cuda, adv_lib):
 
 
 def test_noalloc_stage_allocates_nothing(cuda, adv_lib):
+    """Free device memory is the same before the first call and after the
+    calls: the static array is committed when the handle is created, not by
+    a stage call."""
     torch = cuda
     L, h, n = _setup(adv_lib, torch, degree=3, n_cells=(8, 8, 8))
     try:
         u = torch.from_numpy(np.random.default_rng(1).standard_normal(n)).cuda()
-        r, k = torch.zeros_like(u), torch.zeros_like(u)
+        r, k, v, w = (torch.zeros_like(u) for _ in range(4))
         s = _stream(torch)
-        # the first call on the device looks up the array's address
-        assert L.adv_perform_stage_noalloc(h, 0.0, 0.01, 0.02, _p(u), _p(r), _p(u), _p(r), s) == 0
+        # a stage with no aliasing (which stages nothing) loads the stage
+        # kernel's code on the device, which the driver may place in newly
+        # committed memory
+        assert L.adv_perform_stage(h, 0.0, 0.01, 0.02, _p(v), _p(k), _p(u), _p(w), s) == 0
         torch.cuda.synchronize()
         free_before = torch.cuda.mem_get_info()[0]
         for _ in range(2):
@@ -86,6 +91,23 @@ def test_noalloc_stage_allocates_nothing(cuda, adv_lib):
             assert L.adv_perform_stage_noalloc(h, 0.0, 0.01, 0.02, _p(r), _p(k), _p(u), _p(r), s) == 0
         torch.cuda.synchronize()
         assert torch.cuda.mem_get_info()[0] == free_before
+    finally:
+        L.adv_destroy(h)
+
+
+def test_noalloc_stage_is_timed_like_the_other_entry_points(cuda, adv_lib):
+    torch = cuda
+    L, h, n = _setup(adv_lib, torch, degree=2, n_cells=(4, 4, 4))
+    try:
+        u = torch.from_numpy(np.random.default_rng(2).standard_normal(n)).cuda()
+        r, k = torch.zeros_like(u), torch.zeros_like(u)
+        s = _stream(torch)
+        assert L.adv_set_timing(h, 1) == 0
+        for _ in range(3):
+            assert L.adv_perform_stage_noalloc(h, 0.0, 0.01, 0.02, _p(u), _p(r), _p(u), _p(r), s) == 0
+        sec, calls = ctypes.c_double(), ctypes.c_int64()
+        assert L.adv_timing(h, ctypes.byref(sec), ctypes.byref(calls)) == 0
+        assert calls.value == 3 and sec.value > 0.0
     finally:
         L.adv_destroy(h)
 
