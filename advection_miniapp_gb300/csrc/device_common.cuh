@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../../include/advection_gb300.h"
 
 namespace adv
@@ -66,6 +68,26 @@ static inline cudaError_t upload_tables_local(const DevTables<double> *d, const 
   return cudaMemcpyToSymbol(c_tab_f, f, sizeof(c_tab_f));
 }
 
+// One-time opt-in of a kernel's dynamic shared-memory size on the current
+// device (a per-device function attribute).  The mask of configured devices
+// is atomic because handles on different host threads may launch the same
+// kernel concurrently; two threads that both see the bit clear both set the
+// attribute, which is harmless.  Devices 64 and up set it on every launch.
+template <typename K>
+inline cudaError_t opt_in_smem(K kernel, int bytes, std::atomic<unsigned long long> &configured)
+{
+  int         dev = 0;
+  cudaError_t e   = cudaGetDevice(&dev);
+  if (e != cudaSuccess)
+    return e;
+  if (dev < 64 && ((configured.load(std::memory_order_acquire) >> dev) & 1ull))
+    return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess && dev < 64)
+    configured.fetch_or(1ull << dev, std::memory_order_acq_rel);
+  return e;
+}
+
 template <typename T>
 __device__ __forceinline__ const DevTables<T> &tab(int n);
 template <>
@@ -81,28 +103,37 @@ __device__ __forceinline__ const DevTables<float> &tab<float>(int n)
 
 // binary64 -> binary32 by integer arithmetic (round half away from zero in
 // magnitude; |x| below the smallest normal binary32 flushes to a signed
-// zero).  On this GPU F2F conversions issue on the FP64 pipe, which the
-// FP32-operator path otherwise reserves for the FP64 vector updates.
+// zero; |x| >= 2^128 and infinities give a signed infinity, as does a
+// rounding that carries past the largest binary32; NaN gives a quiet NaN).
+// On this GPU F2F conversions issue on the FP64 pipe, which the FP32-operator
+// path otherwise reserves for the FP64 vector updates.
 __device__ __forceinline__ float d2f_int(double x)
 {
-  const long long b  = __double_as_longlong(x);
-  const unsigned  hi = (unsigned)((unsigned long long)b >> 32);
-  const unsigned  lo = (unsigned)b;
+  const long long b   = __double_as_longlong(x);
+  const unsigned  hi  = (unsigned)((unsigned long long)b >> 32);
+  const unsigned  lo  = (unsigned)b;
+  const unsigned  ahi = hi & 0x7FFFFFFFu;
   // exponent and top 23 mantissa bits, exponent rebased from 1023 to 127
   const unsigned mag = __funnelshift_l(lo, hi, 3) + ((lo >> 28) & 1u) - 0xC0000000u;
-  const unsigned r   = ((hi & 0x7FF00000u) < 0x38100000u) ? 0u : mag;
+  unsigned       r   = ahi < 0x38100000u ? 0u : mag;
+  // binary64 exponent >= 1151 (|x| >= 2^128), infinity or NaN
+  if (ahi >= 0x47F00000u)
+    r = (ahi > 0x7FF00000u || (ahi == 0x7FF00000u && lo != 0u)) ? 0x7FC00000u : 0x7F800000u;
   return __uint_as_float(r | (hi & 0x80000000u));
 }
 
-// binary32 -> binary64, exact for normal numbers; subnormals become zero.
+// binary32 -> binary64, exact for normal numbers, infinities and NaN (the
+// payload keeps its leading bits); subnormals become zero.
 __device__ __forceinline__ double f2d_int(float f)
 {
   const unsigned b    = __float_as_uint(f);
   const unsigned a    = b & 0x7FFFFFFFu;
   const unsigned sign = b & 0x80000000u;
   const bool     zero = a < 0x00800000u;
-  const unsigned hi   = zero ? sign : (sign | ((a >> 3) + 0x38000000u));
-  const unsigned lo   = zero ? 0u : (b << 29);
+  unsigned       hi   = zero ? sign : (sign | ((a >> 3) + 0x38000000u));
+  if (a >= 0x7F800000u)
+    hi = sign | 0x7FF00000u | ((a >> 3) & 0x000FFFFFu);
+  const unsigned lo = zero ? 0u : (b << 29);
   return __hiloint2double((int)hi, (int)lo);
 }
 

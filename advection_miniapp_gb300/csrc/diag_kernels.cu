@@ -378,20 +378,8 @@ constexpr size_t kSmemBytes = kSmemDoubles * sizeof(double);
 template <typename K>
 cudaError_t opt_in(K kernel)
 {
-  static unsigned long long configured = 0;
-  int                       dev        = 0;
-  cudaError_t               e          = cudaGetDevice(&dev);
-  if (e != cudaSuccess)
-    return e;
-  if (dev >= 64 || !((configured >> dev) & 1ull))
-    {
-      e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
-      if (e != cudaSuccess)
-        return e;
-      if (dev < 64)
-        configured |= 1ull << dev;
-    }
-  return cudaSuccess;
+  static std::atomic<unsigned long long> configured{0};
+  return opt_in_smem(kernel, (int)kSmemBytes, configured);
 }
 } // namespace
 

@@ -508,19 +508,10 @@ cudaError_t launch_stage_gauss_t(const StageArgs &args, cudaStream_t stream)
 {
   using GS = GaussShape<N, T, UNI, VISC, TR>;
   constexpr auto kernel = gauss_kernel<N, T, UNI, VISC, TR, INC>();
-  static unsigned long long configured = 0;
-  int                       dev        = 0;
-  cudaError_t               e          = cudaGetDevice(&dev);
+  static std::atomic<unsigned long long> configured{0};
+  cudaError_t                            e = opt_in_smem(kernel, GS::SMEM, configured);
   if (e != cudaSuccess)
     return e;
-  if (dev >= 64 || !((configured >> dev) & 1ull))
-    {
-      e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, GS::SMEM);
-      if (e != cudaSuccess)
-        return e;
-      if (dev < 64)
-        configured |= 1ull << dev;
-    }
   const long long blocks = (args.n_cells - args.cell_begin + GS::C - 1) / GS::C;
   kernel<<<(unsigned)blocks, GS::THREADS, GS::SMEM, stream>>>(args);
   return cudaGetLastError();

@@ -897,20 +897,10 @@ cudaError_t launch_stage_t(const StageArgs &args, cudaStream_t stream)
 {
   using SH = StageShape<N, T, UNI, VISC>;
   // the shared-memory opt-in is a per-device function attribute
-  static unsigned long long configured = 0;
-  int                       dev        = 0;
-  cudaError_t               e          = cudaGetDevice(&dev);
+  static std::atomic<unsigned long long> configured{0};
+  cudaError_t                            e = opt_in_smem(stage_kernel<N, T, UNI, VISC>, SH::SMEM, configured);
   if (e != cudaSuccess)
     return e;
-  if (dev >= 64 || !((configured >> dev) & 1ull))
-    {
-      e = cudaFuncSetAttribute(stage_kernel<N, T, UNI, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               SH::SMEM);
-      if (e != cudaSuccess)
-        return e;
-      if (dev < 64)
-        configured |= 1ull << dev;
-    }
   const long long blocks = (args.n_cells - args.cell_begin + SH::C - 1) / SH::C;
   stage_kernel<N, T, UNI, VISC><<<(unsigned)blocks, SH::THREADS, SH::SMEM_NODAL, stream>>>(args);
   return cudaGetLastError();

@@ -256,7 +256,11 @@ def test_operator_golden_fixtures(cuda, adv_lib):
 
 
 def test_fp32_operator_l2_error_matches_fp64(cuda, adv_lib):
-    """FP32 operator with FP64 vectors: same L2 error as FP64 within 1.05x (16^3 curved, k=4)."""
+    """FP32 operator with FP64 vectors on a coarse mesh (16^3 curved cells,
+    k=4, 40 steps): same L2 error as FP64 within 1.05x.  This holds only
+    while the discretization error dominates the FP32 round-off; at the
+    bench's 64^3 the ratio is about 12 (test_gpu_at_size records it), and
+    only the FP32 increment form keeps 1.05x there."""
     torch = cuda
     errs = []
     for precision in (0, 1):
@@ -423,3 +427,25 @@ def test_advection_diffusion_workload_reduced(cuda, oracle_mod, adv_lib):
         res[precision] = ud.cpu().numpy()
     assert rel_err(res[0], u) <= FP64_TOL
     assert rel_err(res[1], u) <= 1e-5
+
+
+@pytest.mark.parametrize("bad", [float("inf"), float("-inf"), float("nan"), 1e300, -1e300])
+@pytest.mark.parametrize("case", ["curved-k4", "affine-k3"])
+def test_fp32_operator_propagates_non_finite_input(cuda, adv_lib, case, bad):
+    """The binary64 -> binary32 conversion of the FP32 operator keeps
+    infinities and NaN and turns |x| >= 2^128 into an infinity, so a
+    diverging FP32 run shows non-finite values instead of finite garbage."""
+    torch = cuda
+    g = adv_lib.AdvectionOperation(**CASES[case], precision=adv_lib.PRECISION_FP32_OPERATOR)
+    nq = (CASES[case]["degree"] + 1) ** 3
+    src = np.random.default_rng(3).standard_normal(g.n_dofs)
+    src[nq + 7] = bad  # a DoF of cell 1
+    d = g.initialize_dof_vector()
+    g.apply(to_dev(torch, src), d, 0.0)
+    out = d.cpu().numpy().reshape(-1, nq)
+    assert not np.isfinite(out[1]).all()
+    # a cell that is neither cell 1 (at (1, 0, 0)) nor one of its face
+    # neighbours stays finite: (3, 1, 2) on both meshes
+    nc = CASES[case]["n_cells"]
+    far = 3 + nc[0] * (1 + nc[1] * 2)
+    assert np.isfinite(out[far]).all()
