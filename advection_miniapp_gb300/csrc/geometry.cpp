@@ -92,6 +92,27 @@ double det_inverse(const double *J, double *Ji)
   return det;
 }
 
+// map_grid on the support points relative to the cell's first support point
+// X[0..2], with that point added back to the positions.  The Jacobian is a
+// derivative of the interpolant (the derivative weights sum to zero): summed
+// over absolute coordinates of size ~1 it cancels to entries of size ~h and
+// carries rounding of a few ulps of 1, which depends on the order of the sums
+// (about 4e-13 relative at h = 1/64); relative coordinates are of size ~h,
+// so that rounding drops to a few ulps of the entries themselves.
+void map_grid_rel(int n, double *X, int np0, const double *V0, const double *W0, int np1, const double *V1,
+                  const double *W1, int np2, const double *V2, const double *W2, double *x, double *J)
+{
+  const int    nq    = n * n * n;
+  const double x0[3] = {X[0], X[1], X[2]};
+  for (int p = 0; p < nq; ++p)
+    for (int i = 0; i < 3; ++i)
+      X[3 * p + i] -= x0[i];
+  map_grid(n, X, np0, V0, W0, np1, V1, W1, np2, V2, W2, x, J);
+  for (int p = 0; p < np0 * np1 * np2; ++p)
+    for (int i = 0; i < 3; ++i)
+      x[3 * p + i] += x0[i];
+}
+
 // support points of the cell with global indices (ix, iy, iz)
 void cell_support_points(const adv_config &cfg, const Mesh &m, const Tables1D &tb, int ix, int iy, int iz,
                          double *X)
@@ -268,7 +289,7 @@ void compute_geometry(const adv_config &cfg, const Mesh &m, const Tables1D &tb, 
         for (int64_t c = 0; c < m.n_cells; ++c)
           {
             cell_support_points(cfg, m, tb, c, X.data());
-            map_grid(n, X.data(), n, S, Sd, n, S, Sd, n, S, Sd, x.data(), J.data());
+            map_grid_rel(n, X.data(), n, S, Sd, n, S, Sd, n, S, Sd, x.data(), J.data());
             double *out = &g.cell[(size_t)c * 4 * nq];
             double  vavg[3] = {0.0, 0.0, 0.0}, vol = 0.0;
             for (int q = 0; q < nq; ++q)
@@ -364,8 +385,8 @@ void compute_geometry(const adv_config &cfg, const Mesh &m, const Tables1D &tb, 
                         V[e][q * n + a] = tb.S[q][a], W[e][q * n + a] = tb.Sd[q][a];
                   }
               }
-            map_grid(n, X.data(), np[0], V[0], W[0], np[1], V[1], W[1], np[2], V[2], W[2], x.data(),
-                     J.data());
+            map_grid_rel(n, X.data(), np[0], V[0], W[0], np[1], V[1], W[1], np[2], V[2], W[2], x.data(),
+                         J.data());
             // grid point (p0, p1, p2) -> face point (q1 along t1, q2 along t2)
             for (int q2 = 0; q2 < n; ++q2)
               for (int q1 = 0; q1 < n; ++q1)

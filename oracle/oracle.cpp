@@ -365,6 +365,10 @@ struct Op
         for (int e = 0; e < 3; ++e)
           J[d][e] = 0.0;
       }
+    // sums over the support points relative to the first one: the
+    // derivative weights sum to zero, and on absolute coordinates (size ~1)
+    // the Jacobian (size ~h) would carry rounding of a few ulps of 1 that
+    // depends on the order of the sums
     for (int c2 = 0; c2 < n; ++c2)
       for (int c1 = 0; c1 < n; ++c1)
         for (int c0 = 0; c0 < n; ++c0)
@@ -376,12 +380,15 @@ struct Op
             const double  w2 = v[0][c0] * v[1][c1] * dv[2][c2];
             for (int d = 0; d < 3; ++d)
               {
-                x[d] += w * y[d];
-                J[d][0] += w0 * y[d];
-                J[d][1] += w1 * y[d];
-                J[d][2] += w2 * y[d];
+                const double yr = y[d] - X[d];
+                x[d] += w * yr;
+                J[d][0] += w0 * yr;
+                J[d][1] += w1 * yr;
+                J[d][2] += w2 * yr;
               }
           }
+    for (int d = 0; d < 3; ++d)
+      x[d] += X[d];
   }
 
   static double inverse3(const double J[3][3], double *Ji)

@@ -1,0 +1,245 @@
+"""Parity of the CUDA path with the CPU oracle at the workloads' own sizes.
+
+The other parity tests use meshes of at most 6^3 cells; these run the
+benchmark workloads themselves:
+
+* 64^3 sine-deformed cells of degree 4 (32,768,000 DoFs; the bench
+  workload): the operator at two times, two fused LSRK(5,4) steps in the
+  library's default form (collocation with face traces), one whole anchor
+  block of the FP32 increment form, and the L2 errors of the three precision
+  forms after 100 steps (advection_solver.cc:661-756, 1183-1208);
+* 32^3 affine cells of degree 5 with the rotating field, SIPG diffusion and
+  Dirichlet-zero data (7,077,888 DoFs): the operator on either side of the
+  velocity's sign change and three steps
+  (advection_diffusion_solver.cc:531-613, advection_solver_variable.cc:427-456);
+* 32^3 deformed cells of degree 4 with BDF2 at Courant 8 (4,096,000 DoFs):
+  two implicit steps whose linear systems the oracle re-checks, and the
+  FP32- and FP64-preconditioned solutions side by side
+  (advection_solver_implicit.cc:1457-1525).
+
+Bars as in the other parity tests: FP64 within 1e-12 relative (max norm over
+the largest reference entry), the FP32 increment form within 5e-6, FGMRES
+residuals recomputed by the oracle within 2e-10.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-12
+FP32_TOL = 5e-6
+
+DEFORMED_64 = dict(degree=4, n_cells=(64, 64, 64), mesh_type=1, deformation=0.08)
+DIFFUSION_32 = dict(degree=5, n_cells=(32, 32, 32), periodic=0, velocity_type=1, velocity=(1.0, 1.0, 0.3),
+                    velocity_period=0.5, diffusion=1e-3, penalty_factor=1.0, initial_condition=1,
+                    ic_params=(0.3, 0.5, 0.5, 0.1), boundary_value=0)
+DEFORMED_32 = dict(degree=4, n_cells=(32, 32, 32), mesh_type=1, deformation=0.08)
+
+
+def rel_err(a, ref):
+    return np.abs(np.asarray(a) - ref).max() / max(np.abs(ref).max(), 1e-300)
+
+
+def to_dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def release(torch):
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+
+
+@pytest.fixture(scope="module")
+def oracle_64(oracle_mod):
+    return oracle_mod.Oracle(**DEFORMED_64)
+
+
+def test_presets_are_the_tested_configurations(adv_lib):
+    """The workload presets the bench and run.py use are the configurations
+    tested here."""
+    for name, cfg in (("deformed-k4-64", DEFORMED_64), ("advection-diffusion-k5-32", DIFFUSION_32),
+                      ("deformed-k4-32", DEFORMED_32)):
+        w = adv_lib.workload_config(name)
+        c = adv_lib.make_config(**cfg)
+        for field, _ in w._fields_:
+            a, b = getattr(w, field), getattr(c, field)
+            if hasattr(a, "__len__"):
+                a, b = list(a), list(b)
+            assert a == b, (name, field, a, b)
+
+
+def test_deformed_64_operator(cuda, oracle_64, adv_lib):
+    """The operator on the bench mesh, on seeded random data and on the
+    projected initial data, at two times.
+
+    Random data gives an output of the operator's own size, ||L|| ||u||
+    (derivatives of noise), and is compared within 1e-12 of its largest
+    entry.  Smooth data gives an output (about -a.grad u) some 200 times
+    smaller than the volume and face terms it is the difference of, so the
+    rounding of the metric terms (the Jacobians of the degree-4 mapping,
+    summed in a different order by the oracle and by the library's geometry
+    set-up: a few ulps) shows up amplified relative to that output (measured:
+    1.1e-11 of its largest entry).  Its bar is therefore normwise, 1e-12 of
+    ||L|| ||u|| (||L|| from the random case), plus 5e-11 of its own largest
+    entry, far below any error of the discretization (a wrong metric term or
+    flux shows up at 1e-6 and above)."""
+    torch = cuda
+    o = oracle_64
+    g = adv_lib.AdvectionOperation(adv_lib.workload_config("deformed-k4-64"))
+    assert g.n_dofs == o.n_dofs == 32_768_000
+    rnd = np.random.default_rng(64).standard_normal(o.n_dofs)
+    smooth = o.project(0.0)
+    d = g.initialize_dof_vector()
+    ref_rnd = o.apply(rnd, 0.0)
+    g.apply(to_dev(torch, rnd), d, 0.0)
+    torch.cuda.synchronize()
+    assert rel_err(d.cpu().numpy(), ref_rnd) <= FP64_TOL
+    op_norm = np.abs(ref_rnd).max() / np.abs(rnd).max()
+    for t in (0.0, 0.37):
+        ref = o.apply(smooth, t)
+        g.apply(to_dev(torch, smooth), d, t)
+        torch.cuda.synchronize()
+        diff = np.abs(d.cpu().numpy() - ref).max()
+        assert diff <= FP64_TOL * op_norm * np.abs(smooth).max(), (t, diff)
+        assert diff <= 5e-11 * np.abs(ref).max(), (t, diff / np.abs(ref).max())
+    del g, d
+    release(torch)
+
+
+def test_deformed_64_lsrk_steps(cuda, oracle_64, adv_lib):
+    """Two LSRK(5,4) steps from the projected initial data, as the bench runs
+    them (default form: collocation with face traces, one basis change on
+    entry and one on exit)."""
+    torch = cuda
+    o = oracle_64
+    g = adv_lib.AdvectionOperation(adv_lib.workload_config("deformed-k4-64"))
+    dt = g.time_step(0.5)
+    assert abs(dt - o.time_step(0.5)) <= 1e-15 * dt
+    u = o.project(0.0)
+    r, k = o.zeros(), o.zeros()
+    for s in range(2):
+        o.lsrk_step(s * dt, dt, u, r, k)
+    ud = g.initialize_dof_vector()
+    g.project_initial(ud)
+    rd, kd = g.initialize_dof_vector(), g.initialize_dof_vector()
+    g.lsrk_steps(adv_lib.LSRK_5_4, 0.0, dt, 2, ud, rd, kd)
+    torch.cuda.synchronize()
+    assert rel_err(ud.cpu().numpy(), u) <= FP64_TOL
+    del g, ud, rd, kd
+    release(torch)
+
+
+def test_deformed_64_fp32_increment_block(cuda, oracle_64, adv_lib):
+    """One whole anchor block (4 steps at the default anchor interval) of the
+    FP32 increment form against the oracle's FP64 steps."""
+    torch = cuda
+    o = oracle_64
+    g = adv_lib.AdvectionOperation(adv_lib.workload_config("deformed-k4-64",
+                                                           precision=adv_lib.PRECISION_FP32_INCREMENT))
+    dt = g.time_step(0.5)
+    u = o.project(0.0)
+    r, k = o.zeros(), o.zeros()
+    for s in range(4):
+        o.lsrk_step(s * dt, dt, u, r, k)
+    ud = g.initialize_dof_vector()
+    g.project_initial(ud)
+    rd, kd = g.initialize_dof_vector(), g.initialize_dof_vector()
+    g.lsrk_steps(adv_lib.LSRK_5_4, 0.0, dt, 4, ud, rd, kd)
+    torch.cuda.synchronize()
+    assert rel_err(ud.cpu().numpy(), u) <= FP32_TOL
+    del g, ud, rd, kd
+    release(torch)
+
+
+def test_deformed_64_precision_forms_l2_error(cuda, adv_lib):
+    """L2 errors after 100 steps at 64^3 (what the bench reports): the FP32
+    increment form (anchor every 4 steps) stays within 1.05x of FP64's.  The
+    plain FP32 operator does not at this resolution: its round-off, amplified
+    by the DG derivative, is about 12x the FP64 discretization error (it holds
+    the 1.05x bar only on coarse meshes, see the 16^3 test); this records it."""
+    torch = cuda
+    errs = {}
+    for precision in (adv_lib.PRECISION_FP64, adv_lib.PRECISION_FP32_OPERATOR, adv_lib.PRECISION_FP32_INCREMENT):
+        g = adv_lib.AdvectionOperation(adv_lib.workload_config("deformed-k4-64", precision=precision))
+        dt = g.time_step(0.5)
+        u = g.initialize_dof_vector()
+        g.project_initial(u)
+        r, k = g.initialize_dof_vector(), g.initialize_dof_vector()
+        g.lsrk_steps(adv_lib.LSRK_5_4, 0.0, dt, 100, u, r, k)
+        e, n = g.l2_error(u, 100 * dt)
+        errs[precision] = e / n
+        del g, u, r, k
+        release(torch)
+    ratio_inc = errs[adv_lib.PRECISION_FP32_INCREMENT] / errs[adv_lib.PRECISION_FP64]
+    ratio_op = errs[adv_lib.PRECISION_FP32_OPERATOR] / errs[adv_lib.PRECISION_FP64]
+    assert ratio_inc <= 1.05, errs
+    assert ratio_op > 1.05, errs  # the plain FP32 operator misses the bar at 64^3
+    assert ratio_op < 50, errs
+
+
+def test_advection_diffusion_32(cuda, oracle_mod, adv_lib):
+    """The advection-diffusion workload at its size: the operator at t = 0.1
+    and t = 0.3 (the rotating field's factor cos(pi t / 0.5) changes sign at
+    t = 0.25) and three LSRK(5,4) steps from the projected blob."""
+    torch = cuda
+    o = oracle_mod.Oracle(**DIFFUSION_32)
+    g = adv_lib.AdvectionOperation(adv_lib.workload_config("advection-diffusion-k5-32"))
+    assert g.n_dofs == o.n_dofs == 7_077_888
+    src = np.random.default_rng(32).standard_normal(o.n_dofs)
+    s = to_dev(torch, src)
+    d = g.initialize_dof_vector()
+    for t in (0.1, 0.3):
+        ref = o.apply(src, t)
+        g.apply(s, d, t)
+        torch.cuda.synchronize()
+        assert rel_err(d.cpu().numpy(), ref) <= FP64_TOL, t
+    dt = g.time_step(0.5)
+    assert abs(dt - o.time_step(0.5)) <= 1e-15 * dt
+    # the sign change of the field at t = 0.25 falls inside the second step
+    t0 = 0.25 - 1.5 * dt
+    u = o.project(0.0)
+    r, k = o.zeros(), o.zeros()
+    for st in range(3):
+        o.lsrk_step(t0 + st * dt, dt, u, r, k)
+    ud = g.initialize_dof_vector()
+    g.project_initial(ud)
+    rd, kd = g.initialize_dof_vector(), g.initialize_dof_vector()
+    g.lsrk_steps(adv_lib.LSRK_5_4, t0, dt, 3, ud, rd, kd)
+    torch.cuda.synchronize()
+    assert rel_err(ud.cpu().numpy(), u) <= FP64_TOL
+    del g, s, d, ud, rd, kd
+    release(torch)
+
+
+def test_implicit_bdf2_32(cuda, oracle_mod, adv_lib):
+    """BDF2 at Courant 8 on the implicit workload's mesh: the first (implicit
+    Euler) and the second (BDF2) step; the oracle recomputes each step's
+    residual b - (c M - L) u_new; the FP32- and FP64-preconditioned solutions
+    agree to the solver tolerance."""
+    torch = cuda
+    o = oracle_mod.Oracle(**DEFORMED_32)
+    g = adv_lib.AdvectionOperation(adv_lib.workload_config("deformed-k4-32"))
+    assert g.n_dofs == o.n_dofs == 4_096_000
+    dt = g.time_step(8.0)
+    finals = {}
+    for precision in (adv_lib.PRECISION_FP32_OPERATOR, adv_lib.PRECISION_FP64):
+        s = adv_lib.ImplicitSolver(g, restart=30, precond_precision=precision)
+        u_nm1, u_n, u_new = (g.initialize_dof_vector() for _ in range(3))
+        g.project_initial(u_n)
+        for step in range(2):
+            its = s.bdf2_step((step + 1) * dt, dt, step == 0, u_n, u_nm1, u_new, rel_tol=1e-10)
+            assert 0 < its < 200
+            un, unew = u_n.cpu().numpy(), u_new.cpu().numpy()
+            if step == 0:
+                cm, rhs = 1.0 / dt, un / dt
+            else:
+                cm, rhs = 1.5 / dt, (2.0 * un - 0.5 * u_nm1.cpu().numpy()) / dt
+            b = o.apply_mass(rhs)
+            res = np.linalg.norm(b - o.vmult(unew, cm, (step + 1) * dt)) / np.linalg.norm(b)
+            assert res <= 2e-10, (precision, step, res, its)
+            u_nm1, u_n, u_new = u_n, u_new, u_nm1
+        finals[precision] = u_n.cpu().numpy()
+        s.close()
+        del u_nm1, u_n, u_new
+        release(torch)
+    assert rel_err(finals[adv_lib.PRECISION_FP32_OPERATOR], finals[adv_lib.PRECISION_FP64]) <= 1e-8
