@@ -209,8 +209,23 @@ def run_mix(requests, rate_clock=True, memory_budget_bytes=150 * 10 ** 9, steps_
                "throughput_req_s": len(requests) / wall,
                "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
                "gdof_stages_per_s": work / wall / 1e9, "ticks": stats["ticks"], "launches": stats["launches"],
-               "max_rel_l2_error": max(results[r.index]["rel_l2_error"] for r in requests)}
+               "max_rel_l2_error": max(results[r.index]["rel_l2_error"] for r in requests),
+               "rel_l2_error": error_summary(requests, results)}
     return results, summary, sols
+
+
+def error_summary(requests, results):
+    """Relative L2 errors of the solves (each against its exactly translated
+    initial data): percentiles per precision tag and the whole list in
+    request order."""
+    out = {}
+    for name, tag in (("fp64", PRECISION_FP64), ("fp32_operator", PRECISION_FP32_OPERATOR)):
+        e = np.array([results[r.index]["rel_l2_error"] for r in requests if r.precision == tag])
+        if len(e):
+            out[name] = {"count": int(len(e)), "p50": float(np.percentile(e, 50)),
+                         "p99": float(np.percentile(e, 99)), "max": float(e.max())}
+    out["per_request"] = [float(results[r.index]["rel_l2_error"]) for r in sorted(requests, key=lambda q: q.index)]
+    return out
 
 
 def run_one_at_a_time(requests, rate_clock=True):
@@ -246,7 +261,7 @@ def run_one_at_a_time(requests, rate_clock=True):
     lat = np.array([results[r.index]["latency_s"] for r in requests])
     summary = {"requests": len(requests), "wall_s": wall, "throughput_req_s": len(requests) / wall,
                "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
-               "gdof_stages_per_s": work / wall / 1e9}
+               "gdof_stages_per_s": work / wall / 1e9, "rel_l2_error": error_summary(requests, results)}
     return results, summary
 
 

@@ -16,7 +16,10 @@ one; `e2e` repeats the FP64 measurement through the C ABI's host-buffer entry
 point (adv_lsrk_steps_host), which copies the solution from pinned host memory
 to the device and back around every step; `roofline` and `cpu_baseline`
 explain the numbers; `serving` gives the p50/p99 solve latency of the
-serving loop on a 128-request mix beside one-at-a-time solving.  With
+serving loop at a sustained arrival rate (256 requests of the serving mix,
+FIFO admission) beside one-at-a-time solving; `advection_diffusion` and
+`implicit` measure the two other GPU workloads (32^3 cells of degree 5 with
+SIPG and the rotating field; BDF2 with FGMRES on 32^3 deformed cells).  With
 --gpus N > 1 (torchrun) every rank solves its own replica (the path has no
 data exchange between independent solves): weak scaling.
 
@@ -39,8 +42,15 @@ sys.path.insert(0, ROOT)
 WORKLOAD = "deformed-k4-64"
 WORKLOAD_DESC = ("64^3 sine-deformed cells (amplitude 0.08), degree 4, 32,768,000 DoFs, "
                  "velocity (1, 0.15, -0.05), periodic, upwind, LSRK(5,4), Courant 0.5/k^1.5")
+
 METRIC = "GDoF/s per LSRK stage, FP64 vs FP32-op at equal L2 error; p50/p99 solve latency"
 STAGES = 5
+
+
+def config_dict():
+    c = dict(CONFIG)
+    c["workload"] = f"{WORKLOAD}: {WORKLOAD_DESC}"
+    return c
 
 
 def parse():
@@ -52,6 +62,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--no-workloads", action="store_true",
+                   help="skip the advection-diffusion and implicit workloads")
     return p.parse_args()
 
 
@@ -131,7 +143,13 @@ def fp_work_per_cell(n, curved=True, stage=True, collocation=False, traces=False
 # kernels, from ncu captures of the 40^3 curved degree-4 case (8,000,000 DoFs,
 # vectors and geometry larger than L2; profiles/ has the commands), scaled to
 # the workload by the DoF count
-NCU_TRAFFIC_PER_DOF = {"fp64": (543.862016e6 + 175.197184e6) / 8.0e6, "fp32": (297.32096e6 + 94.11456e6) / 8.0e6}
+NCU_TRAFFIC_PER_DOF = {"fp64": (543.862016e6 + 175.197184e6) / 8.0e6, "fp32": (297.32096e6 + 94.11456e6) / 8.0e6,
+                       # FP32 increment stage (stage_gauss_kernel<5, float, ..., INC>), the block's
+                       # dominant kernel: 19 of the 21 launches of a 4-step block
+                       "fp32_increment": (312.3e6 + 67.1e6) / 8.0e6}
+
+# the bench workload's config dict, identical in both arms
+CONFIG = {"workload": None, "l2": "inputs larger than L2 (three 262 MB FP64 vectors + geometry per stage)"}
 
 
 def increment_bytes_per_dof_step(n, interval=4, stages=STAGES):
@@ -266,7 +284,7 @@ def reference_arm(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": res["seconds"] / res["steps"] * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded analytic initial data)",
-        "config": {"workload": f"{WORKLOAD}: {WORKLOAD_DESC}", "arm": "CPU oracle (C++ FP64 restatement, OpenMP)"},
+        "config": config_dict(), "arm": "CPU oracle (C++ FP64 restatement, OpenMP)",
         "cpu_baseline": {"value": round(res["gdofs"], 5), "unit": "GDoF/s", "cores": res["threads"],
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(res["gdofs"], 5), "unit": "GDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -338,22 +356,132 @@ def e2e_fp64(torch, adv, args, stream):
     return dict(value=op.n_dofs * STAGES * args.steps / sec / 1e9, h2d=nb, d2h=nb)
 
 
-def serving_run(n_requests=128, rate=200.0):
-    """p50/p99 solve latency of the serving loop: the seeded request mix of
-    the serving workload (meshes of 4^3 to 32^3 cells, degrees 2-6, end
-    times 0.1-1, FP64 or FP32 operator), Poisson arrivals, shortest-first
-    admission of at most 16 solves at once, beside the same requests solved
-    one at a time in arrival order."""
+def l2_distance(torch, op, a, b):
+    """Relative L2 distance ||a - b|| / ||b|| of two solutions as finite-element
+    functions (norms through the mass matrix)."""
+    d = a - b
+    md = op.initialize_dof_vector()
+    op.apply_mass(d, md)
+    mb = op.initialize_dof_vector()
+    op.apply_mass(b, mb)
+    return float(torch.dot(d, md).sqrt() / torch.dot(b, mb).sqrt())
+
+
+def advection_diffusion_run(torch, adv, stream, sampler_index, t_end=0.5):
+    """The advection-diffusion workload (32^3 affine cells of degree 5,
+    7,077,888 DoFs, rotating field times cos(pi t / 0.5), SIPG with
+    diffusivity 1e-3 and penalty (k+1)^2/h, Dirichlet-zero data, Gaussian blob
+    of width 0.1 at (0.3, 0.5, 0.5)): LSRK(5,4) to t = 0.5 with the FP64
+    operator and with the FP32 operator (FP64 vectors), timed with CUDA
+    events, and the L2 distance between the two final solutions."""
+    out, sols = {}, {}
+    for name, precision in (("fp64", adv.PRECISION_FP64), ("fp32_operator", adv.PRECISION_FP32_OPERATOR)):
+        op = adv.AdvectionOperation(adv.workload_config("advection-diffusion-k5-32", precision=precision))
+        dt = op.time_step(0.5)
+        steps = max(1, int(-(-t_end // dt)))
+        dt = t_end / steps
+        u = op.initialize_dof_vector()
+        op.project_initial(u)
+        r, k = op.initialize_dof_vector(), op.initialize_dof_vector()
+        torch.cuda.synchronize()
+        with ClockSampler(sampler_index) as clk, torch.cuda.stream(stream):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            n0 = op.launch_count()
+            e0.record(stream)
+            op.lsrk_steps(adv.LSRK_5_4, 0.0, dt, steps, u, r, k, stream=stream)
+            e1.record(stream)
+            e1.synchronize()
+            launches = op.launch_count() - n0
+        sec = e0.elapsed_time(e1) / 1e3
+        out[name] = {"value": round(op.n_dofs * STAGES * steps / sec / 1e9, 4), "unit": "GDoF/s",
+                     "ms_per_step": round(sec / steps * 1e3, 4), "steps": steps, "kernel_launches": launches,
+                     "clocks": clk.summary()}
+        sols[name] = (op, u)
+        del r, k
+    op64, u64 = sols["fp64"]
+    out["fp32_speedup_vs_fp64"] = round(out["fp32_operator"]["value"] / out["fp64"]["value"], 3)
+    out["l2_distance_fp32_vs_fp64"] = l2_distance(torch, op64, sols["fp32_operator"][1], u64)
+    out["n_dofs"] = op64.n_dofs
+    out["t_end"] = t_end
+    out["workload"] = ("advection-diffusion-k5-32: 32^3 affine cells, degree 5, 7,077,888 DoFs, rotating field "
+                       "x cos(pi t / 0.5), SIPG nu = 1e-3, penalty (k+1)^2/h, Dirichlet-zero data, Gaussian blob "
+                       "(width 0.1 at (0.3, 0.5, 0.5)), LSRK(5,4) to t = 0.5")
+    del sols
+    torch.cuda.empty_cache()
+    return out
+
+
+def implicit_run(torch, adv, stream, sampler_index, steps=50):
+    """The implicit workload (32^3 deformed cells of degree 4, 4,096,000
+    DoFs, the 8^3 workload's velocity and initial data): BDF2 at Courant
+    number 8 with FGMRES(30) to a relative tolerance of 1e-10, the block-Jacobi
+    FDM preconditioner in FP32 and, for the reference run, in FP64; iterations
+    per step, time per step (CUDA events) and the L2 distance between the two
+    solutions (advection_solver_implicit.cc:1865-1870 prints the iterations)."""
+    op = adv.AdvectionOperation(adv.workload_config("deformed-k4-32"))
+    dt = op.time_step(8.0)
+    out, sols = {}, {}
+    for name, precision in (("fp32_precond", adv.PRECISION_FP32_OPERATOR), ("fp64_precond", adv.PRECISION_FP64)):
+        s = adv.ImplicitSolver(op, restart=30, precond_precision=precision)
+        u_nm1, u_n, u_new = (op.initialize_dof_vector() for _ in range(3))
+        op.project_initial(u_n)
+        its = []
+        torch.cuda.synchronize()
+        with ClockSampler(sampler_index) as clk, torch.cuda.stream(stream):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            n0 = op.launch_count()
+            e0.record(stream)
+            for step in range(steps):
+                its.append(s.bdf2_step((step + 1) * dt, dt, step == 0, u_n, u_nm1, u_new, rel_tol=1e-10,
+                                       stream=stream))
+                u_nm1, u_n, u_new = u_n, u_new, u_nm1
+            e1.record(stream)
+            e1.synchronize()
+            launches = op.launch_count() - n0
+        sec = e0.elapsed_time(e1) / 1e3
+        err, nrm = op.l2_error(u_n, steps * dt)
+        out[name] = {"iterations_per_step": round(sum(its) / steps, 3), "ms_per_step": round(sec / steps * 1e3, 3),
+                     "rel_l2_error_vs_exact": err / nrm, "kernel_launches": launches, "clocks": clk.summary()}
+        sols[name] = u_n
+        s.close()
+    out["l2_distance_fp32_vs_fp64_precond"] = l2_distance(torch, op, sols["fp32_precond"], sols["fp64_precond"])
+    out.update(steps=steps, dt=dt, courant=8.0, n_dofs=op.n_dofs,
+               workload="deformed-k4-32: 32^3 sine-deformed cells, degree 4, 4,096,000 DoFs, BDF2 (BDF1 first "
+                        "step) at Courant 8, FGMRES(30) rel. tol. 1e-10, block-Jacobi FDM preconditioner")
+    del sols, op
+    torch.cuda.empty_cache()
+    return out
+
+
+# Poisson arrival rate at which the serving loop is measured: the highest
+# rate of the sweep in profiles/serving_sustained.md whose p99 latency stays
+# within the bound below (the GPU serves about 11 requests/s of this mix)
+SUSTAINED_RATE = 8.0
+P99_BOUND_S = 10.0
+
+
+def serving_run(n_requests=256, rate=SUSTAINED_RATE):
+    """p50/p99 solve latency (arrival to completion) of the serving loop at a
+    sustained Poisson arrival rate: the seeded request mix of the serving
+    workload (meshes of 4^3 to 32^3 cells, degrees 2-6, end times 0.1-1,
+    FP64 or FP32 operator), FIFO admission under the 150 GB budget, beside
+    the same requests solved one at a time in arrival order at the same
+    rate.  Each solve's relative L2 error against its exact solution is
+    reported (percentiles per precision, and the list)."""
     from advection_miniapp_gb300 import serving as srv_mod
     reqs = srv_mod.request_mix(n_requests, 0, rate)
-    _, srv, _ = srv_mod.run_mix(reqs, rate_clock=True, max_active=16, policy="shortest")
+    _, srv, _ = srv_mod.run_mix(reqs, rate_clock=True, policy="fifo")
     _, base = srv_mod.run_one_at_a_time(reqs, rate_clock=True)
     keep = ("p50_latency_s", "p99_latency_s", "throughput_req_s", "gdof_stages_per_s", "wall_s")
     server = {k: round(srv[k], 4) for k in keep}
-    server.update(failed=srv["failed"], max_rel_l2_error=srv["max_rel_l2_error"])
-    return {"requests": n_requests, "rate_req_s": rate, "admission": "shortest-first, 16 solves at once",
-            "latency": "arrival to completion", "server": server,
-            "one_at_a_time": {k: round(base[k], 4) for k in keep}}
+    server.update(failed=srv["failed"], ticks=srv["ticks"], kernel_launches=srv["launches"],
+                  rel_l2_error=srv["rel_l2_error"])
+    one = {k: round(base[k], 4) for k in keep}
+    one["rel_l2_error"] = {k: v for k, v in base["rel_l2_error"].items() if k != "per_request"}
+    return {"sustained_rate_req_s": rate, "p99_bound_s": P99_BOUND_S,
+            "p99_within_bound": bool(srv["p99_latency_s"] <= P99_BOUND_S),
+            "requests": n_requests, "admission": "FIFO under a 150 GB device-memory budget",
+            "latency": "arrival to completion", "server": server, "one_at_a_time": one}
 
 
 def ours(args):
@@ -452,6 +580,10 @@ def ours(args):
     serving = None
     if not args.no_serving and world == 1:
         serving = serving_run()
+    adv_diff = implicit = None
+    if not args.no_workloads:
+        adv_diff = advection_diffusion_run(torch, adv, stream, dev_index)
+        implicit = implicit_run(torch, adv, stream, dev_index)
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -473,9 +605,8 @@ def ours(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded analytic initial data on the deformed mesh; no dataset)",
-        "config": {"workload": f"{WORKLOAD}: {WORKLOAD_DESC}", "precision": "FP64 operator, FP64 vectors",
-                   "l2": "inputs larger than L2 (three 262 MB FP64 vectors + geometry per stage)",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "config": config_dict(), "precision": "FP64 operator, FP64 vectors",
+        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
         "rel_l2_error": r64["rel_l2"],
         "roofline": {"bound": "fp64", "achieved": round(achieved64, 4), "peak": round(fp64_peak, 4),
                      "unit": "TFLOP/s", "frac": round(achieved64 / fp64_peak, 4),
@@ -511,13 +642,18 @@ def ours(args):
                     "start u_a and 19 FP32 operator evaluations on the increments r - u_a (u - u_a - C K0 kept in "
                     "FP64, the operator input in binary32); collocation basis",
             "roofline": {"bound": "hbm", "achieved": round(inc_gbs, 2), "peak": hbm_peak, "unit": "GB/s",
-                         "frac": round(inc_gbs / hbm_peak, 4), "traffic": None,
+                         "frac": round(inc_gbs / hbm_peak, 4),
+                         "traffic": traffic(NCU_TRAFFIC_PER_DOF["fp32_increment"], n_dofs),
+                         "traffic_definition": "DRAM bytes of one FP32 increment stage launch (the block's "
+                                               "dominant kernel), ncu at 40^3 scaled by the DoFs",
                          "bytes_per_dof_step": round(increment_bytes_per_dof_step(n), 2),
                          "definition": "algorithmic vector and geometry bytes of a 4-step block (one FP64 anchor "
                                        "and 19 FP32 stages) over the block's time"},
             "clocks": rinc["clocks"]},
         "e2e": e2e,
         "serving": serving,
+        "advection_diffusion": adv_diff,
+        "implicit": implicit,
         "gpu_launches": r64["launches"] + r32["launches"] + rinc["launches"],
         "clocks": r64["clocks"],
         "cpu_baseline": cpu,
