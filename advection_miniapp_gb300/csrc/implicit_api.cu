@@ -41,10 +41,15 @@ int alloc(void **p, size_t bytes, int64_t &count)
   return ADV_OK;
 }
 
-int launch_vmult(adv_handle *h, const double *src, double *dst, double mass_factor, double t, cudaStream_t s)
+// gauss: src holds values at the Gauss points and dst receives the dual
+// coefficients on the Gauss-point basis (the collocation-form stage kernel,
+// no interpolation or integration sweeps); else both are on the nodal basis
+int launch_vmult(adv_handle *h, const double *src, double *dst, double mass_factor, double t, cudaStream_t s,
+                 bool gauss = false)
 {
   adv::StageArgs A = adv::detail::base_args(*h, t);
   A.mode           = adv::kModeVmult;
+  A.gauss          = gauss ? 1 : 0;
   A.r_in           = src;
   A.r_out          = dst;
   A.mass_factor    = mass_factor;
@@ -214,6 +219,37 @@ int adv_solver_device_bytes(const adv_solver *S, int64_t *out)
   return ADV_OK;
 }
 
+} // extern "C"
+
+namespace
+{
+// block-Jacobi FDM preconditioner; gauss: residual as dual coefficients and
+// result as values on the Gauss-point basis
+int precondition(adv_solver *S, const double *src, double *dst, double mass_factor, double t, cudaStream_t s,
+                 bool gauss)
+{
+  adv_handle  *h = S->h;
+  adv::FdmArgs A;
+  std::memset(&A, 0, sizeof(A));
+  A.src         = src;
+  A.dst         = dst;
+  A.n_cells     = h->mesh.n_cells;
+  A.mass_factor = mass_factor;
+  A.time_factor = time_factor_of(*h, t);
+  A.gauss       = gauss ? 1 : 0;
+  const void *cell = S->precond_precision == ADV_PRECISION_FP64 ? (const void *)h->d_fdm_cell_d
+                                                                 : (const void *)h->d_fdm_cell_f;
+  ADV_CUDA(adv::launch_fdm(h->mesh.n, S->precond_precision, A, S->d_tables, cell, s));
+  ++h->launches;
+  return ADV_OK;
+}
+
+int fgmres(adv_solver *S, double mass_factor, double t, const double *rhs, double *x, double rel_tol,
+           int max_iterations, int *iterations, double *rel_residual, cudaStream_t s, bool gauss);
+} // namespace
+
+extern "C" {
+
 int adv_precondition(adv_solver *S, const double *src, double *dst, double mass_factor, double t, void *stream)
 {
   adv::detail::CallTrace trace_(S ? S->h : nullptr, "adv_precondition", (cudaStream_t)stream);
@@ -221,20 +257,9 @@ int adv_precondition(adv_solver *S, const double *src, double *dst, double mass_
     return fail(ADV_ERR_INVALID, "null argument");
   if (src == dst)
     return fail(ADV_ERR_ALIASING, "adv_precondition: dst must not alias src");
-  adv_handle *h = S->h;
-  if (int e = adv::detail::check_device(h))
+  if (int e = adv::detail::check_device(S->h))
     return e;
-  adv::FdmArgs A;
-  A.src         = src;
-  A.dst         = dst;
-  A.n_cells     = h->mesh.n_cells;
-  A.mass_factor = mass_factor;
-  A.time_factor = time_factor_of(*h, t);
-  const void *cell = S->precond_precision == ADV_PRECISION_FP64 ? (const void *)h->d_fdm_cell_d
-                                                                 : (const void *)h->d_fdm_cell_f;
-  ADV_CUDA(adv::launch_fdm(h->mesh.n, S->precond_precision, A, S->d_tables, cell, (cudaStream_t)stream));
-  ++h->launches;
-  return ADV_OK;
+  return precondition(S, src, dst, mass_factor, t, (cudaStream_t)stream, false);
 }
 
 int adv_fgmres(adv_solver *S, double mass_factor, double t, const double *rhs, double *x, double rel_tol,
@@ -245,13 +270,29 @@ int adv_fgmres(adv_solver *S, double mass_factor, double t, const double *rhs, d
     return fail(ADV_ERR_INVALID, "null argument");
   if (rhs == x)
     return fail(ADV_ERR_ALIASING, "adv_fgmres: x must not alias rhs");
-  adv_handle *h = S->h;
-  if (int e = adv::detail::check_device(h))
+  if (int e = adv::detail::check_device(S->h))
     return e;
-  cudaStream_t s  = (cudaStream_t)stream;
-  const int    m  = S->restart;
-  const int64_t n = S->n;
-  double      *c1 = S->d_small, *c2 = S->d_small + (m + 1), *nrm = S->d_small + 2 * (m + 1),
+  return fgmres(S, mass_factor, t, rhs, x, rel_tol, max_iterations, iterations, rel_residual, (cudaStream_t)stream,
+                false);
+}
+
+} // extern "C"
+
+namespace
+{
+// FGMRES(m), right-preconditioned, CGS2.  gauss: rhs and the residuals are
+// dual coefficients and x holds values on the Gauss-point basis; the
+// iteration measures residuals in that basis but stops on the nodal
+// residual ||S^T r|| / ||S^T rhs|| <= rel_tol (S^T = S^T x S^T x S^T), the
+// criterion of the nodal solve, checked exactly whenever the Gauss-basis
+// residual is below its own tolerance (which tightens if the check fails).
+int fgmres(adv_solver *S, double mass_factor, double t, const double *rhs, double *x, double rel_tol,
+           int max_iterations, int *iterations, double *rel_residual, cudaStream_t s, bool gauss)
+{
+  adv_handle   *h  = S->h;
+  const int     m  = S->restart;
+  const int64_t n  = S->n;
+  double       *c1 = S->d_small, *c2 = S->d_small + (m + 1), *nrm = S->d_small + 2 * (m + 1),
          *ydev = S->d_small + 2 * (m + 1) + 1;
   double bnorm = 0.0;
   if (int e = norm2(S, rhs, &bnorm, s))
@@ -267,22 +308,47 @@ int adv_fgmres(adv_solver *S, double mass_factor, double t, const double *rhs, d
         *rel_residual = 0.0;
       return ADV_OK;
     }
+  // the nodal norm of a dual vector on the Gauss-point basis (through S->w)
+  auto nodal_norm = [&](const double *v, double *out) -> int {
+    ADV_CUDA(cudaMemcpyAsync(S->w, v, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    ADV_CUDA(adv::launch_basis_dual_to_nodal(h->mesh.n, S->w, 0, h->mesh.n_cells, s));
+    ++h->launches;
+    return norm2(S, S->w, out, s);
+  };
+  double bnorm_nodal = bnorm, tol = rel_tol;
+  if (gauss)
+    if (int e = nodal_norm(rhs, &bnorm_nodal))
+      return e;
   std::vector<double> H((m + 1) * m), cs(m), sn(m), g(m + 1), y(m), hh(2 * (m + 1) + 1);
   bool                converged = false;
   while (true)
     {
       // r = rhs - A x into V_0
-      if (int e = launch_vmult(h, x, S->w, mass_factor, t, s))
+      if (int e = launch_vmult(h, x, S->w, mass_factor, t, s, gauss))
         return e;
       ADV_CUDA(adv::launch_lincomb(S->V, 1.0, rhs, -1.0, S->w, n, s));
       double beta = 0.0;
       if (int e = norm2(S, S->V, &beta, s))
         return e;
       res = beta / bnorm;
-      if (res <= rel_tol)
+      if (res <= tol)
         {
-          converged = true;
-          break;
+          if (!gauss)
+            {
+              converged = true;
+              break;
+            }
+          double rn = 0.0;
+          if (int e = nodal_norm(S->V, &rn))
+            return e;
+          const double res_nodal = rn / bnorm_nodal;
+          if (res_nodal <= rel_tol)
+            {
+              res       = res_nodal;
+              converged = true;
+              break;
+            }
+          tol = res * 0.5 * rel_tol / res_nodal;
         }
       if (its >= max_iterations)
         break;
@@ -294,9 +360,9 @@ int adv_fgmres(adv_solver *S, double mass_factor, double t, const double *rhs, d
       for (int j = 0; j < m && its < max_iterations; ++j)
         {
           double *vj = S->V + j * n, *zj = S->Z + j * n;
-          if (int e = adv_precondition(S, vj, zj, mass_factor, t, stream))
+          if (int e = precondition(S, vj, zj, mass_factor, t, s, gauss))
             return e;
-          if (int e = launch_vmult(h, zj, S->w, mass_factor, t, s))
+          if (int e = launch_vmult(h, zj, S->w, mass_factor, t, s, gauss))
             return e;
           // classical Gram-Schmidt, twice
           ADV_CUDA(adv::launch_multi_dot(S->V, n, j + 1, S->w, n, S->d_partials, c1, s));
@@ -328,7 +394,7 @@ int adv_fgmres(adv_solver *S, double mass_factor, double t, const double *rhs, d
           ++its;
           k   = j + 1;
           res = std::fabs(g[j + 1]) / bnorm;
-          if (res <= rel_tol || hn == 0.0)
+          if (res <= tol || hn == 0.0)
             break;
           if (j + 1 < m)
             ADV_CUDA(adv::launch_lincomb(S->V + (j + 1) * n, 1.0 / hn, S->w, 0.0, nullptr, n, s));
@@ -353,6 +419,9 @@ int adv_fgmres(adv_solver *S, double mass_factor, double t, const double *rhs, d
     return fail(ADV_ERR_NOT_CONVERGED, "FGMRES reached the iteration limit, relative residual " + std::to_string(res));
   return ADV_OK;
 }
+} // namespace
+
+extern "C" {
 
 int adv_bdf2_step(adv_solver *S, double t_new, double dt, int first_step, const double *u_n, const double *u_nm1,
                   double *u_new, double rel_tol, int *iterations, void *stream)
@@ -364,26 +433,49 @@ int adv_bdf2_step(adv_solver *S, double t_new, double dt, int first_step, const 
     return fail(ADV_ERR_ALIASING, "u_new must not alias u_n or u_nm1");
   if (!(dt > 0.0))
     return fail(ADV_ERR_INVALID, "dt must be positive");
-  adv_handle  *h = S->h;
-  cudaStream_t s = (cudaStream_t)stream;
-  const int64_t n = S->n;
+  adv_handle *h = S->h;
+  if (int e = adv::detail::check_device(h))
+    return e;
+  cudaStream_t    s  = (cudaStream_t)stream;
+  const int64_t   n  = S->n;
+  const int       nn = h->mesh.n;
+  const long long nc = h->mesh.n_cells;
+  // The system (c M - L) u_new = M rhs is solved on the Gauss-point basis:
+  // values at the Gauss points for u, dual coefficients for the residuals.
+  // There the mass matrix is diag(JxW), the operator is the collocation-form
+  // stage kernel in weak form and the FDM preconditioner needs no basis
+  // transforms; the stopping rule is the nodal relative residual.
+  // S->tmp: u_n on the Gauss points; u_new: u_nm1 on the Gauss points, then
+  // the initial guess and the solution, changed back to nodal values at the end
+  ADV_CUDA(cudaMemcpyAsync(S->tmp, u_n, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  ADV_CUDA(adv::launch_basis_change(nn, S->tmp, 0, nc, true, s));
+  ++h->launches;
+  const double *geo = h->mesh.uniform ? nullptr : static_cast<const double *>(h->d_cell_geo);
+  const double  vol = h->mesh.h[0] * h->mesh.h[1] * h->mesh.h[2];
   double        cm;
-  // right-hand side M tmp: BDF1 on the first step, BDF2 afterwards
   if (first_step)
     {
+      // BDF1: (M / dt - L) u_new = M u_n / dt, initial guess u_n
       cm = 1.0 / dt;
-      ADV_CUDA(adv::launch_lincomb(S->tmp, 1.0 / dt, u_n, 0.0, nullptr, n, s));
-      ADV_CUDA(cudaMemcpyAsync(u_new, u_n, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      ADV_CUDA(adv::launch_gauss_mass_lincomb(nn, S->b, 1.0 / dt, S->tmp, 0.0, nullptr, nc, geo, vol, s));
+      ADV_CUDA(cudaMemcpyAsync(u_new, S->tmp, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
     }
   else
     {
+      // BDF2: (3/(2 dt) M - L) u_new = M (2 u_n - u_nm1 / 2) / dt, initial
+      // guess 2 u_n - u_nm1
       cm = 1.5 / dt;
-      ADV_CUDA(adv::launch_lincomb(S->tmp, 2.0 / dt, u_n, -0.5 / dt, u_nm1, n, s));
-      ADV_CUDA(adv::launch_lincomb(u_new, 2.0, u_n, -1.0, u_nm1, n, s)); // extrapolated initial guess
+      ADV_CUDA(cudaMemcpyAsync(u_new, u_nm1, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      ADV_CUDA(adv::launch_basis_change(nn, u_new, 0, nc, true, s));
+      ++h->launches;
+      ADV_CUDA(adv::launch_gauss_mass_lincomb(nn, S->b, 2.0 / dt, S->tmp, -0.5 / dt, u_new, nc, geo, vol, s));
+      ADV_CUDA(adv::launch_lincomb(u_new, 2.0, S->tmp, -1.0, u_new, n, s));
     }
-  if (int e = launch_mass_op(h, S->tmp, S->b, s))
-    return e;
-  return adv_fgmres(S, cm, t_new, S->b, u_new, rel_tol, 100000, iterations, nullptr, stream);
+  h->launches += 2;
+  const int rc = fgmres(S, cm, t_new, S->b, u_new, rel_tol, 100000, iterations, nullptr, s, true);
+  ADV_CUDA(adv::launch_basis_change(nn, u_new, 0, nc, false, s));
+  ++h->launches;
+  return rc;
 }
 
 } // extern "C"

@@ -14,6 +14,8 @@
 // preconditioner's precision (FP32 by default) in shared memory.
 #include "implicit_kernels.h"
 
+#include <algorithm>
+
 namespace adv
 {
 namespace
@@ -61,7 +63,10 @@ __device__ __forceinline__ void csweep(const T *Mr, const T *Mi, const T (&xr)[N
     }
 }
 
-template <int N, typename T>
+// GAUSS: the residual and the result are on the Gauss-point basis (the
+// residual as dual coefficients, the result as values at the points): the
+// transforms S^{-T} on entry and S^{-1} on exit drop out.
+template <int N, typename T, bool GAUSS>
 __global__ void __launch_bounds__(FdmShape<N>::THREADS)
   fdm_kernel(const FdmArgs A, const T *__restrict__ tables, const T *__restrict__ cell_data)
 {
@@ -99,7 +104,11 @@ __global__ void __launch_bounds__(FdmShape<N>::THREADS)
 #pragma unroll
       for (int k = 0; k < N; ++k)
         in[k] = (T)__ldg(g + k * NF);
-      rsweep<N, T>(tb.SiT, in, out);
+      if (GAUSS)
+        for (int k = 0; k < N; ++k)
+          out[k] = in[k];
+      else
+        rsweep<N, T>(tb.SiT, in, out);
 #pragma unroll
       for (int k = 0; k < N; ++k)
         R[cl * NQ + r + k * NF] = out[k];
@@ -114,7 +123,11 @@ __global__ void __launch_bounds__(FdmShape<N>::THREADS)
 #pragma unroll
       for (int k = 0; k < N; ++k)
         in[k] = p[k * N];
-      rsweep<N, T>(tb.SiT, in, out);
+      if (GAUSS)
+        for (int k = 0; k < N; ++k)
+          out[k] = in[k];
+      else
+        rsweep<N, T>(tb.SiT, in, out);
 #pragma unroll
       for (int k = 0; k < N; ++k)
         p[k * N] = out[k];
@@ -130,7 +143,11 @@ __global__ void __launch_bounds__(FdmShape<N>::THREADS)
 #pragma unroll
       for (int k = 0; k < N; ++k)
         in[k] = p[k];
-      rsweep<N, T>(tb.SiT, in, xr);
+      if (GAUSS)
+        for (int k = 0; k < N; ++k)
+          xr[k] = in[k];
+      else
+        rsweep<N, T>(tb.SiT, in, xr);
 #pragma unroll
       for (int k = 0; k < N; ++k)
         xi[k] = T(0);
@@ -217,7 +234,11 @@ __global__ void __launch_bounds__(FdmShape<N>::THREADS)
         xr[k] = p[k], xi[k] = pi[k];
       const int s = sgn[cl * 3 + 0];
       csweep<N, T>(Vr(s), Vi(s), xr, xi, yr, yi);
-      rsweep<N, T>(tb.Si, yr, out);
+      if (GAUSS)
+        for (int k = 0; k < N; ++k)
+          out[k] = yr[k];
+      else
+        rsweep<N, T>(tb.Si, yr, out);
 #pragma unroll
       for (int k = 0; k < N; ++k)
         p[k] = out[k];
@@ -232,7 +253,11 @@ __global__ void __launch_bounds__(FdmShape<N>::THREADS)
 #pragma unroll
       for (int k = 0; k < N; ++k)
         in[k] = p[k * N];
-      rsweep<N, T>(tb.Si, in, out);
+      if (GAUSS)
+        for (int k = 0; k < N; ++k)
+          out[k] = in[k];
+      else
+        rsweep<N, T>(tb.Si, in, out);
 #pragma unroll
       for (int k = 0; k < N; ++k)
         p[k * N] = out[k];
@@ -247,7 +272,11 @@ __global__ void __launch_bounds__(FdmShape<N>::THREADS)
 #pragma unroll
       for (int k = 0; k < N; ++k)
         in[k] = p[k * NF];
-      rsweep<N, T>(tb.Si, in, out);
+      if (GAUSS)
+        for (int k = 0; k < N; ++k)
+          out[k] = in[k];
+      else
+        rsweep<N, T>(tb.Si, in, out);
       double *d = A.dst + (cell0 + cl) * NQ + r;
 #pragma unroll
       for (int k = 0; k < N; ++k)
@@ -467,12 +496,16 @@ cudaError_t launch_fdm(int n, int precision, const FdmArgs &a, const void *table
   case NN:                                                                                                     \
     {                                                                                                          \
       const unsigned blocks = (unsigned)((a.n_cells + FdmShape<NN>::C - 1) / FdmShape<NN>::C);               \
-      if (precision == 0)                                                                                      \
-        fdm_kernel<NN, double><<<blocks, FdmShape<NN>::THREADS, 0, s>>>(                                      \
-          a, static_cast<const double *>(tables), static_cast<const double *>(cell_data));                    \
+      const double *td = static_cast<const double *>(tables), *cd = static_cast<const double *>(cell_data);    \
+      const float  *tf = static_cast<const float *>(tables), *cf = static_cast<const float *>(cell_data);      \
+      if (precision == 0 && a.gauss)                                                                           \
+        fdm_kernel<NN, double, true><<<blocks, FdmShape<NN>::THREADS, 0, s>>>(a, td, cd);                     \
+      else if (precision == 0)                                                                                 \
+        fdm_kernel<NN, double, false><<<blocks, FdmShape<NN>::THREADS, 0, s>>>(a, td, cd);                    \
+      else if (a.gauss)                                                                                        \
+        fdm_kernel<NN, float, true><<<blocks, FdmShape<NN>::THREADS, 0, s>>>(a, tf, cf);                      \
       else                                                                                                     \
-        fdm_kernel<NN, float><<<blocks, FdmShape<NN>::THREADS, 0, s>>>(a, static_cast<const float *>(tables), \
-                                                                        static_cast<const float *>(cell_data)); \
+        fdm_kernel<NN, float, false><<<blocks, FdmShape<NN>::THREADS, 0, s>>>(a, tf, cf);                     \
       break;                                                                                                   \
     }
   switch (n)
@@ -537,6 +570,50 @@ cudaError_t launch_lincomb(double *dst, double a, const double *x, double b, con
                            cudaStream_t s)
 {
   lincomb_kernel<<<vec_blocks(n), kVecThreads, 0, s>>>(dst, a, x, b, y, n);
+  return cudaGetLastError();
+}
+
+namespace
+{
+// dst = JxW (a x + b y) at every Gauss point (y may be null), grid-stride over
+// the points; JxW = w_q / idet_q from the cell geometry, or w_q V (uniform)
+template <int N>
+__global__ void __launch_bounds__(kVecThreads)
+  gauss_mass_lincomb_kernel(double *dst, double a, const double *x, double b, const double *y, long long n_cells,
+                            const double *cell_geo, double vol)
+{
+  constexpr int            NQ = N * N * N;
+  const DevTables<double> &tb = tab<double>(N);
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n_cells * NQ;
+       e += (long long)gridDim.x * blockDim.x)
+    {
+      const long long c   = e / NQ;
+      const int       q   = (int)(e - c * NQ);
+      const double    w   = tb.gw[q % N] * tb.gw[(q / N) % N] * tb.gw[q / (N * N)];
+      const double    jxw = cell_geo ? w / __ldg(cell_geo + c * 4 * NQ + 3 * NQ + q) : w * vol;
+      double          v   = a * __ldg(x + e);
+      if (y)
+        v = fma(b, __ldg(y + e), v);
+      dst[e] = jxw * v;
+    }
+}
+} // namespace
+
+cudaError_t launch_gauss_mass_lincomb(int n, double *dst, double a, const double *x, double b, const double *y,
+                                      long long n_cells, const double *cell_geo, double vol, cudaStream_t s)
+{
+  const long long total  = n_cells * n * n * n;
+  const unsigned  blocks = (unsigned)std::min<long long>((total + kVecThreads - 1) / kVecThreads, 152 * 16);
+  switch (n)
+    {
+      case 2: gauss_mass_lincomb_kernel<2><<<blocks, kVecThreads, 0, s>>>(dst, a, x, b, y, n_cells, cell_geo, vol); break;
+      case 3: gauss_mass_lincomb_kernel<3><<<blocks, kVecThreads, 0, s>>>(dst, a, x, b, y, n_cells, cell_geo, vol); break;
+      case 4: gauss_mass_lincomb_kernel<4><<<blocks, kVecThreads, 0, s>>>(dst, a, x, b, y, n_cells, cell_geo, vol); break;
+      case 5: gauss_mass_lincomb_kernel<5><<<blocks, kVecThreads, 0, s>>>(dst, a, x, b, y, n_cells, cell_geo, vol); break;
+      case 6: gauss_mass_lincomb_kernel<6><<<blocks, kVecThreads, 0, s>>>(dst, a, x, b, y, n_cells, cell_geo, vol); break;
+      case 7: gauss_mass_lincomb_kernel<7><<<blocks, kVecThreads, 0, s>>>(dst, a, x, b, y, n_cells, cell_geo, vol); break;
+      default: return cudaErrorInvalidValue;
+    }
   return cudaGetLastError();
 }
 } // namespace adv

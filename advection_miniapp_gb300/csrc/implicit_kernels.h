@@ -14,6 +14,7 @@ struct FdmArgs
   long long     n_cells;
   double        mass_factor; // c in (c M + A)
   double        time_factor; // velocity factor s of the rotating field (1 for constant)
+  int           gauss;       // residual and result on the Gauss-point basis (no S^{-T}, S^{-1} transforms)
 };
 
 struct MassArgs
@@ -41,4 +42,9 @@ cudaError_t launch_multi_axpy(double *w, const double *V, long long ld, int m, c
                               long long n, cudaStream_t s);
 cudaError_t launch_lincomb(double *dst, double a, const double *x, double b, const double *y, long long n,
                            cudaStream_t s);
+// dst = JxW (a x + b y) at the Gauss points of every cell (y may be null): the
+// mass matrix on the Gauss-point basis, diagonal; cell_geo holds idet = 1 /
+// det J per point (field case) or is null for a uniform mesh of cell volume vol
+cudaError_t launch_gauss_mass_lincomb(int n, double *dst, double a, const double *x, double b, const double *y,
+                                      long long n_cells, const double *cell_geo, double vol, cudaStream_t s);
 } // namespace adv

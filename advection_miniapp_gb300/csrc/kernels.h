@@ -94,7 +94,9 @@ cudaError_t launch_stage(int n, int precision, const StageArgs &args, cudaStream
 // hold the values at the (k+1)^3 Gauss points of every cell, the nodal basis
 // of the Lagrange polynomials on those points.  The operator is the same
 // polynomial map as the Gauss-Lobatto nodal form without its interpolation
-// and inverse-mass sweeps.  Modes: apply, stage, last stage.
+// and inverse-mass sweeps.  Modes: apply, stage, last stage, and the
+// implicit operator in weak form (vmult): r_out receives the dual
+// coefficients on the Gauss-point basis, JxW (c u - L u) at each point.
 cudaError_t launch_stage_gauss_fp64(int n, const StageArgs &args, cudaStream_t stream);
 cudaError_t launch_stage_gauss_fp32(int n, const StageArgs &args, cudaStream_t stream);
 cudaError_t upload_tables_gauss64(const DevTables<double> *d, const DevTables<float> *f);
@@ -106,6 +108,12 @@ cudaError_t upload_tables_gauss32(const DevTables<double> *d, const DevTables<fl
 // (width 2: values and reference normal derivatives, for SIPG).
 cudaError_t launch_basis_change(int n, double *u, long long cell_begin, long long cell_end, bool to_gauss,
                                 cudaStream_t stream, double *traces = nullptr, int width = 1);
+// In-place u <- (S^T x S^T x S^T) u for the cells [cell_begin, cell_end): the
+// dual coefficients of a weak-form vector on the Gauss-point basis to those
+// on the Gauss-Lobatto nodal basis (each nodal function is the combination
+// sum_q S[q][i] l_q of the Gauss-point Lagrange functions).
+cudaError_t launch_basis_dual_to_nodal(int n, double *u, long long cell_begin, long long cell_end,
+                                       cudaStream_t stream);
 // Face traces [6][width][n^2] per cell of the Gauss-point values in u (the
 // values at the face points, with width 2 also the reference normal
 // derivatives), for the cells [cell_begin, cell_end); u is not changed.

@@ -356,9 +356,25 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
       for (int k = 0; k < N; ++k)
         {
           T zz = z[k * NF] + out[k];
+          const long long gi = gb + k * NF;
+          if (A.mode == kModeVmult)
+            {
+              // implicit operator in weak form on the Gauss-point basis (dual
+              // coefficients, the rows of the Lagrange functions on the Gauss
+              // points): JxW (c U - L-bracket), the bracket taken before the
+              // inverse Jacobian determinant; JxW = w / idet (field) or w V
+              // (uniform)
+              const T wq = tb.gw[r % N] * tb.gw[r / N] * tb.gw[k];
+              const T br = Consts<T>::out(A) * zz;
+              const T cm = Consts<T>::mass(A);
+              const T v  = UNI ? wq * Consts<T>::vol(A) * (cm * U[k] - br)
+                               : wq * (cm * U[k] / G[3 * NQ + r + k * NF] - br);
+              A.r_out[gi] = to_double<T>(v);
+              next[k]     = 0.0;
+              continue;
+            }
           if (!UNI)
             zz *= G[3 * NQ + r + k * NF];
-          const long long gi = gb + k * NF;
           double          kd = to_double<T>(zz);
           if (INC)
             {

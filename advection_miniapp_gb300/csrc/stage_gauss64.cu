@@ -9,7 +9,8 @@ namespace
 // u <- (M x M x M) u per cell, M = S (to the Gauss points) or S^-1, through
 // shared memory: one thread per pencil, C cells per CTA.  MODE 1: to the
 // Gauss points (optionally with the face traces of the result), 0: back to
-// the Gauss-Lobatto nodes, 2: only the face traces of u (no change of basis).
+// the Gauss-Lobatto nodes, 2: only the face traces of u (no change of basis),
+// 3: M = S^T (dual coefficients from the Gauss-point to the nodal basis).
 template <int N, int MODE>
 __global__ void __launch_bounds__(StageShape<N, double, true, false>::THREADS)
   basis_kernel(double *u, long long cell_begin, long long cell_end, double *traces, int width)
@@ -44,6 +45,8 @@ __global__ void __launch_bounds__(StageShape<N, double, true, false>::THREADS)
             in[k] = p[k * st];
           if (TO_GAUSS)
             sweep2<N, double, false>(tb.S, tb.S_eo, in, out);
+          else if (MODE == 3)
+            sweep2<N, double, false>(tb.St, tb.St_eo, in, out);
           else
             sweep2<N, double, false>(tb.Si, tb.Si_eo, in, out);
 #pragma unroll
@@ -95,6 +98,8 @@ cudaError_t launch_basis_n(double *u, long long cell_begin, long long cell_end, 
     basis_kernel<N, 1><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, traces, width);
   else if (mode == 2)
     basis_kernel<N, 2><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, traces, width);
+  else if (mode == 3)
+    basis_kernel<N, 3><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, nullptr, 1);
   else
     basis_kernel<N, 0><<<(unsigned)blocks, SH::THREADS, 0, s>>>(u, cell_begin, cell_end, nullptr, 1);
   return cudaGetLastError();
@@ -133,6 +138,12 @@ cudaError_t launch_basis_change(int n, double *u, long long cell_begin, long lon
                                 cudaStream_t stream, double *traces, int width)
 {
   return launch_basis_mode(n, u, cell_begin, cell_end, to_gauss ? 1 : 0, stream, traces, width);
+}
+
+cudaError_t launch_basis_dual_to_nodal(int n, double *u, long long cell_begin, long long cell_end,
+                                       cudaStream_t stream)
+{
+  return launch_basis_mode(n, u, cell_begin, cell_end, 3, stream, nullptr, 1);
 }
 
 cudaError_t launch_face_traces(int n, const double *u, long long cell_begin, long long cell_end,

@@ -127,3 +127,36 @@ def test_bdf2_second_order_in_time(cuda, adv_lib):
     e1 = run_bdf2(adv_lib, g, dt, 8)
     e2 = run_bdf2(adv_lib, g, dt / 2, 16)
     assert e1 / e2 > 3.2, (e1, e2)
+
+
+@pytest.mark.parametrize("case", ["curved-k4", "rotating-k3", "affine-k2-dirichlet"])
+def test_bdf2_step_equals_nodal_fgmres_solve(cuda, oracle_mod, adv_lib, case):
+    """adv_bdf2_step solves on the Gauss-point basis (values at the Gauss
+    points, residuals as dual coefficients there, the collocation-form
+    operator and the FDM preconditioner without its basis transforms) and
+    stops on the nodal residual.  Its implicit-Euler and BDF2 steps equal a
+    nodal FGMRES solve (adv_fgmres) of the same systems, and the oracle
+    confirms the nodal residuals."""
+    cfg = CASES[case]
+    o = oracle_mod.Oracle(**cfg)
+    g = adv_lib.AdvectionOperation(**cfg)
+    s = adv_lib.ImplicitSolver(g, restart=30, precond_precision=0)
+    dt = g.time_step(4.0)
+    u0 = g.initialize_dof_vector()
+    g.project_initial(u0)
+    u1, u2 = g.initialize_dof_vector(), g.initialize_dof_vector()
+    s.bdf2_step(dt, dt, True, u0, None, u1, rel_tol=1e-12)
+    s.bdf2_step(2 * dt, dt, False, u1, u0, u2, rel_tol=1e-12)
+    # the same systems through the nodal solver
+    m0, x1 = g.initialize_dof_vector(), u0.clone()
+    g.apply_mass(u0 / dt, m0)
+    s.fgmres(1.0 / dt, dt, m0, x1, rel_tol=1e-12, max_iterations=2000)
+    assert rel(u1, x1.cpu().numpy()) <= 1e-9
+    m1, x2 = g.initialize_dof_vector(), 2 * u1 - u0
+    g.apply_mass((2.0 * u1 - 0.5 * u0) / dt, m1)
+    s.fgmres(1.5 / dt, 2 * dt, m1, x2, rel_tol=1e-12, max_iterations=2000)
+    assert rel(u2, x2.cpu().numpy()) <= 1e-9
+    for unew, cm, rhs, t in ((u1, 1.0 / dt, u0.cpu().numpy() / dt, dt),
+                             (u2, 1.5 / dt, (2.0 * u1.cpu().numpy() - 0.5 * u0.cpu().numpy()) / dt, 2 * dt)):
+        b = o.apply_mass(rhs)
+        assert np.linalg.norm(b - o.vmult(unew.cpu().numpy(), cm, t)) / np.linalg.norm(b) <= 2e-12
