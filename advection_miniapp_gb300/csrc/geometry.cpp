@@ -401,8 +401,9 @@ void compute_geometry(const adv_config &cfg, const Mesh &m, const Tables1D &tb, 
                       const double det = det_inverse(&J[9 * gpt], Ji);
                       velocity_field(cfg, &x[3 * gpt], b);
                       const double cc = det * (Ji[3 * d + 0] * b[0] + Ji[3 * d + 1] * b[1] + Ji[3 * d + 2] * b[2]);
-                      g.face[d][(size_t)f * 2 * nf + fq]      = 0.5 * (cc + alpha * std::fabs(cc));
-                      g.face[d][(size_t)f * 2 * nf + nf + fq] = 0.5 * (cc - alpha * std::fabs(cc));
+                      // (P, M) pairs per face point: one 16-byte load in the kernels
+                      g.face[d][(size_t)f * 2 * nf + 2 * fq]     = 0.5 * (cc + alpha * std::fabs(cc));
+                      g.face[d][(size_t)f * 2 * nf + 2 * fq + 1] = 0.5 * (cc - alpha * std::fabs(cc));
                     }
                   if (need_x && boundary)
                     for (int i = 0; i < 3; ++i)

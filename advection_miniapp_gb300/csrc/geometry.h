@@ -57,7 +57,7 @@ struct HostGeometry
   double idet_const = 0.0;
   // field case: per cell [vt0 | vt1 | vt2 | idet] blocks of n^3 values
   std::vector<double> cell;
-  // field case: per direction, per face [P | M] blocks of n^2 values
+  // field case: per direction, per face n^2 (P, M) pairs (one per face point)
   std::vector<double> face[3];
   // Dirichlet: per direction, per face, n^2 points x 3 coordinates (boundary faces only hold data)
   std::vector<double> face_x[3];

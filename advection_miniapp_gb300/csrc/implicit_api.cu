@@ -9,6 +9,7 @@
 // basis and update; the block-Jacobi FDM preconditioner runs in FP32 or FP64.
 // One host synchronisation per iteration (the new Hessenberg column and the
 // norm come back together).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -30,6 +31,11 @@ struct adv_solver
   double     *d_partials = nullptr;
   void       *d_tables   = nullptr;
   int64_t     bytes      = 0;
+  // Gauss-basis solves: the Gauss-basis tolerance as a fraction of the nodal
+  // one, from the ratio of the two relative residuals of the last solve (the
+  // systems of consecutive time steps are alike), so that the nodal check at
+  // convergence rarely fails and forces a restart
+  double      gauss_tol_scale = 1.0;
 };
 
 namespace
@@ -315,7 +321,7 @@ int fgmres(adv_solver *S, double mass_factor, double t, const double *rhs, doubl
     ++h->launches;
     return norm2(S, S->w, out, s);
   };
-  double bnorm_nodal = bnorm, tol = rel_tol;
+  double bnorm_nodal = bnorm, tol = gauss ? rel_tol * S->gauss_tol_scale : rel_tol;
   if (gauss)
     if (int e = nodal_norm(rhs, &bnorm_nodal))
       return e;
@@ -342,6 +348,8 @@ int fgmres(adv_solver *S, double mass_factor, double t, const double *rhs, doubl
           if (int e = nodal_norm(S->V, &rn))
             return e;
           const double res_nodal = rn / bnorm_nodal;
+          if (res_nodal > 0.0)
+            S->gauss_tol_scale = std::min(1.0, std::max(1.0 / 64.0, 0.9 * res / res_nodal));
           if (res_nodal <= rel_tol)
             {
               res       = res_nodal;

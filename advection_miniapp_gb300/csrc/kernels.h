@@ -54,7 +54,7 @@ struct StageArgs
   float         volf;        // uniform case: cell volume (det J)
   double        vol;
   const void   *cell_geo;    // field case: [vt0|vt1|vt2|idet] x n^3 per cell (T)
-  const void   *face_geo[3]; // field case: [P|M] x n^2 per face (T)
+  const void   *face_geo[3]; // field case: n^2 (P, M) pairs per face (T)
   const double *face_x[3];   // Dirichlet faces: n^2 x 3 coordinates per face
   double        t;           // time of the Dirichlet data
   // collocation form with face traces: per cell [6][n^2] values at the face

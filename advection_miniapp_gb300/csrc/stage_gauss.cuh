@@ -140,7 +140,7 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
     return Gb + cl * 4 * NQ;
   };
 
-  // face coefficients [P | M] of face j of local cell cl: staged or global
+  // face coefficients, (P, M) pairs, of face j of local cell cl: staged or global
   auto faces = [&](int cl, int j) -> const T * {
     if (FG)
       {
@@ -162,9 +162,23 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
       }
     else
       {
-        const double *src = A.r_in + cell0 * NQ;
-        for (int i = tid; i < ncell * NQ; i += NT)
-          Ub[i] = from_double<T>(__ldg(src + i));
+        // 16-byte loads of pairs of values (a first value alone when the
+        // range starts off a 16-byte boundary, a last one when one is left)
+        const double *src  = A.r_in + cell0 * NQ;
+        const int     tot  = ncell * NQ;
+        const int     head = (reinterpret_cast<uintptr_t>(src) & 15) ? 1 : 0;
+        const int     np   = (tot - head) / 2;
+        if (tid == 0 && head)
+          Ub[0] = from_double<T>(__ldg(src));
+        if (tid == 1 && head + 2 * np < tot)
+          Ub[tot - 1] = from_double<T>(__ldg(src + tot - 1));
+        const double2 *src2 = reinterpret_cast<const double2 *>(src + head);
+        for (int i = tid; i < np; i += NT)
+          {
+            const double2 v      = __ldg(src2 + i);
+            Ub[head + 2 * i]     = from_double<T>(v.x);
+            Ub[head + 2 * i + 1] = from_double<T>(v.y);
+          }
       }
     if (TR && !TG)
       {

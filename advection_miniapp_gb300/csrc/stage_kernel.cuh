@@ -29,6 +29,8 @@
 
 #include <cuda_pipeline.h>
 
+#include <type_traits>
+
 #include "kernels.h"
 
 namespace adv
@@ -236,7 +238,7 @@ __device__ __forceinline__ void sweep2(const T (&M)[kMaxNDev][kMaxNDev], const E
 
 // Face terms and volume term of one direction d for one pencil of Gauss-point
 // values U along d; returns the pencil's contribution to Z (without 1/det J).
-// Flo / Fhi: [P | M] coefficients of the low / high face (field case);
+// Flo / Fhi: (P, M) pairs of the low / high face (field case);
 // vt: det J (J^{-1} a)_d along the pencil (field case).  VISC adds the SIPG
 // terms of an affine mesh (advection_diffusion_solver.cc:531-613 in the
 // right-hand-side sign convention): dnlo / dnhi are the neighbour's reference
@@ -292,8 +294,12 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
     }
   else
     {
-      Plo = Flo[fq], Mlo = Flo[NF + fq];
-      Phi = Fhi[fq], Mhi = Fhi[NF + fq];
+      // (P, M) pairs per face point, 2 sizeof(T)-aligned
+      using T2      = typename std::conditional<sizeof(T) == sizeof(double), double2, float2>::type;
+      const T2 pmlo = *reinterpret_cast<const T2 *>(Flo + 2 * fq);
+      const T2 pmhi = *reinterpret_cast<const T2 *>(Fhi + 2 * fq);
+      Plo = pmlo.x, Mlo = pmlo.y;
+      Phi = pmhi.x, Mhi = pmhi.y;
     }
   if (A.swap_pm)
     {
@@ -559,7 +565,7 @@ __device__ __forceinline__ void stage_cta(const StageArgs &A, const long long ce
   //      copies of the geometry; they land while the sweeps below run
   if (!UNI)
     geometry_async<N, T>(A, cell0, ncell, s_face, Gb, Fb, tid, NT, !FG);
-  // face coefficients [P | M] of face j of local cell cl: staged or global
+  // face coefficients, (P, M) pairs, of face j of local cell cl: staged or global
   auto faces = [&](int cl, int j) -> const T * {
     if (FG)
       {

@@ -265,6 +265,55 @@ def run_one_at_a_time(requests, rate_clock=True):
     return results, summary
 
 
+def launch_overhead(cases=((4, 2), (8, 4), (16, 4))):
+    """Per-launch cost of small solves: one FP64 request of n^3 cells of
+    degree k through the single-mesh step loop (stream launches, timed with
+    CUDA events and on the host clock) and through the server (graph-captured
+    ticks of 8 or 32 steps, alone or 16 copies batched in one group), as host
+    wall time per kernel launch of the tick graphs."""
+    import torch
+
+    from . import AdvectionOperation, LSRK_5_4
+    out = {}
+    for n, k in cases:
+        r = Request(0, n, k, (0.6, -0.48, 0.64), (0.1, 0.2, 0.3), 4.0 if n == 4 else 1.0, PRECISION_FP64)
+        steps = r.steps()
+        dt = r.t_end / steps
+        op = AdvectionOperation(r.config())
+        u, rr, kk = (op.initialize_dof_vector() for _ in range(3))
+        op.project_initial(u)
+        op.lsrk_steps(LSRK_5_4, 0.0, dt, 10, u, rr, kk)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = op.launch_count()
+        t0 = time.perf_counter()
+        e0.record()
+        op.lsrk_steps(LSRK_5_4, 0.0, dt, steps, u, rr, kk)
+        e1.record()
+        e1.synchronize()
+        wall = time.perf_counter() - t0
+        nl = op.launch_count() - n0
+        res = {"steps": steps, "n_dofs": r.n_dofs, "stream_launches": nl,
+               "stream_us_per_launch_device": e0.elapsed_time(e1) * 1e3 / nl,
+               "stream_us_per_launch_wall": wall * 1e6 / nl}
+        op.close()
+        for spt in (8, 32):
+            for copies in (1, 16):
+                with Server(steps_per_tick=spt) as srv:
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    for _ in range(copies):
+                        srv.submit(r)
+                    srv.drain()
+                    torch.cuda.synchronize()
+                    wall = time.perf_counter() - t0
+                    st = srv.stats()
+                res[f"server_spt{spt}_x{copies}"] = {"wall_s": wall, "ticks": st["ticks"], "launches": st["launches"],
+                                                     "us_per_graph_node": wall * 1e6 / st["launches"]}
+        out[f"{n}^3 k{k}"] = res
+    return out
+
+
 def main(argv=None):
     p = argparse.ArgumentParser(description="serving-loop measurement on one GPU")
     p.add_argument("--requests", type=int, default=256)
@@ -276,7 +325,12 @@ def main(argv=None):
     p.add_argument("--policy", choices=sorted(POLICIES), default="fifo", help="admission order")
     p.add_argument("--t-max", type=float, default=1.0, help="upper end of the end-time range [0.1, t_max]")
     p.add_argument("--baseline", action="store_true", help="also run the requests one at a time")
+    p.add_argument("--overhead", action="store_true",
+                   help="only measure the per-launch cost of small solves (stream launches vs tick graphs)")
     args = p.parse_args(argv)
+    if args.overhead:
+        print(json.dumps(launch_overhead()))
+        return
     reqs = request_mix(args.requests, args.seed, args.rate or None, t_range=(0.1, args.t_max))
     _, summary, _ = run_mix(reqs, rate_clock=bool(args.rate), memory_budget_bytes=int(args.budget_gb * 1e9),
                             steps_per_tick=args.steps_per_tick, max_active=args.max_active, policy=args.policy)
