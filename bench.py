@@ -454,8 +454,9 @@ def implicit_run(torch, adv, stream, sampler_index, steps=50):
 
 
 # Poisson arrival rate at which the serving loop is measured: the highest
-# rate of the sweep in profiles/serving_sustained.md whose p99 latency stays
-# within the bound below (the GPU serves about 11 requests/s of this mix)
+# rate of a sweep (512 requests of the mix at 2, 4, ..., 12 requests/s, FIFO)
+# whose p99 latency stayed within the bound below; the GPU serves about
+# 9.5-9.8 requests/s of this mix
 SUSTAINED_RATE = 8.0
 P99_BOUND_S = 10.0
 
