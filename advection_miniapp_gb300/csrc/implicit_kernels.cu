@@ -379,49 +379,45 @@ __global__ void __launch_bounds__(FdmShape<N>::THREADS) mass_kernel(const MassAr
 // ---------------------------------------------------------------- FP64 vectors
 constexpr int kVecThreads = 256;
 
-// partials[b * m + i] = sum over block b's range of V_i . w  (V_i = V + i * ld)
+// partials[b * m + i] = sum over block b's elements of V_i . w (V_i = V +
+// i * ld), one basis vector at a time: each is a plain coalesced stream
+// (evict-first loads), four elements per thread in flight per step, and w,
+// read once per vector, stays in L2 while the basis vectors stream past.
+// Per vector one block reduction in a fixed order, so results repeat.
 __global__ void __launch_bounds__(kVecThreads)
   multi_dot_kernel(const double *__restrict__ V, long long ld, int m, const double *__restrict__ w, long long n,
                    double *partials)
 {
-  // partial sums of <V_i, w> over this block's chunk: up to 8 products per
-  // pass kept in registers, so each vector element is read once and w once
-  // per pass; then one block reduction per pass
-  constexpr int     G = 8;
-  __shared__ double red[G][kVecThreads / 32];
-  const long long   chunk = (n + gridDim.x - 1) / gridDim.x;
-  const long long   lo = blockIdx.x * chunk, hi = min(n, lo + chunk);
+  __shared__ double red[kVecThreads / 32];
   const int         lane = threadIdx.x % 32, warp = threadIdx.x / 32;
-  for (int i0 = 0; i0 < m; i0 += G)
+  const long long   stride = (long long)gridDim.x * blockDim.x;
+  const long long   first  = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  for (int i = 0; i < m; ++i)
     {
-      const int g = min(G, m - i0);
-      double    s[G];
-#pragma unroll
-      for (int j = 0; j < G; ++j)
-        s[j] = 0.0;
-      for (long long e = lo + threadIdx.x; e < hi; e += blockDim.x)
+      const double *v  = V + i * ld;
+      double        s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+      long long     e  = first;
+      for (; e + 3 * stride < n; e += 4 * stride)
         {
-          const double we = __ldg(w + e);
-#pragma unroll
-          for (int j = 0; j < G; ++j)
-            if (j < g)
-              s[j] = fma(__ldg(V + (i0 + j) * ld + e), we, s[j]);
+          s0 = fma(__ldcs(v + e), __ldg(w + e), s0);
+          s1 = fma(__ldcs(v + e + stride), __ldg(w + e + stride), s1);
+          s2 = fma(__ldcs(v + e + 2 * stride), __ldg(w + e + 2 * stride), s2);
+          s3 = fma(__ldcs(v + e + 3 * stride), __ldg(w + e + 3 * stride), s3);
         }
-#pragma unroll
-      for (int j = 0; j < G; ++j)
-        {
-          for (int o = 16; o > 0; o >>= 1)
-            s[j] += __shfl_down_sync(0xffffffffu, s[j], o);
-          if (lane == 0)
-            red[j][warp] = s[j];
-        }
+      for (; e < n; e += stride)
+        s0 = fma(__ldcs(v + e), __ldg(w + e), s0);
+      double t = (s0 + s1) + (s2 + s3);
+      for (int o = 16; o > 0; o >>= 1)
+        t += __shfl_down_sync(0xffffffffu, t, o);
+      if (lane == 0)
+        red[warp] = t;
       __syncthreads();
-      if (threadIdx.x < g)
+      if (threadIdx.x == 0)
         {
-          double t = 0.0;
+          double b = 0.0;
           for (int k = 0; k < kVecThreads / 32; ++k)
-            t += red[threadIdx.x][k];
-          partials[blockIdx.x * m + i0 + threadIdx.x] = t;
+            b += red[k];
+          partials[blockIdx.x * m + i] = b;
         }
       __syncthreads();
     }
@@ -464,7 +460,7 @@ __global__ void __launch_bounds__(kVecThreads)
     {
       double s = w[e];
       for (int i = 0; i < m; ++i)
-        s = fma(c[i], __ldg(V + i * ld + e), s);
+        s = fma(c[i], __ldcs(V + i * ld + e), s);
       w[e] = s;
     }
 }
@@ -553,7 +549,10 @@ int vec_partial_blocks(long long n)
 cudaError_t launch_multi_dot(const double *V, long long ld, int m, const double *w, long long n, double *partials,
                              double *out, cudaStream_t s)
 {
-  const int blocks = vec_blocks(n);
+  // about 16 elements per thread and vector between two block reductions
+  // (at most vec_blocks(n) blocks, the size of the partials)
+  const long long want   = (n + 16 * kVecThreads - 1) / (16 * kVecThreads);
+  const int       blocks = (int)std::max<long long>(1, std::min<long long>(want, std::min(vec_blocks(n), 152 * 6)));
   multi_dot_kernel<<<blocks, kVecThreads, 0, s>>>(V, ld, m, w, n, partials);
   reduce_partials_kernel<<<m, kVecThreads, 0, s>>>(partials, blocks, m, out);
   return cudaGetLastError();
