@@ -371,7 +371,9 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
         {
           T zz = z[k * NF] + out[k];
           const long long gi = gb + k * NF;
-          if (A.mode == kModeVmult)
+          // (the implicit solver runs the FP64 operator without traces; the
+          // other variants do not carry this branch and its registers)
+          if (!TR && !INC && sizeof(T) == sizeof(double) && A.mode == kModeVmult)
             {
               // implicit operator in weak form on the Gauss-point basis (dual
               // coefficients, the rows of the Lagrange functions on the Gauss
