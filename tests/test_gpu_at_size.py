@@ -125,6 +125,13 @@ def test_deformed_64_lsrk_steps(cuda, oracle_64, adv_lib):
     g.lsrk_steps(adv_lib.LSRK_5_4, 0.0, dt, 2, ud, rd, kd)
     torch.cuda.synchronize()
     assert rel_err(ud.cpu().numpy(), u) <= FP64_TOL
+    # the L2 error against the analytic solution (QGauss(k+2), as the
+    # reference prints it): the two errors differ by at most the distance of
+    # the two solutions, about 1e-12 of the solution's norm
+    e_o, n_o = o.l2_error(u, 2 * dt)
+    e_g, n_g = g.l2_error(ud, 2 * dt)
+    assert abs(n_g - n_o) <= 1e-12 * n_o
+    assert abs(e_g - e_o) <= 1e-11 * n_o, (e_g / n_g, e_o / n_o)
     del g, ud, rd, kd
     release(torch)
 
