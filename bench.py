@@ -143,10 +143,10 @@ def fp_work_per_cell(n, curved=True, stage=True, collocation=False, traces=False
 # kernels, from ncu captures of the 40^3 curved degree-4 case (8,000,000 DoFs,
 # vectors and geometry larger than L2; profiles/ has the commands), scaled to
 # the workload by the DoF count
-NCU_TRAFFIC_PER_DOF = {"fp64": (544.2496e6 + 175.507456e6) / 8.0e6, "fp32": (297.32096e6 + 94.11456e6) / 8.0e6,
+NCU_TRAFFIC_PER_DOF = {"fp64": (544.2496e6 + 175.507456e6) / 8.0e6, "fp32": (297.173248e6 + 95.730432e6) / 8.0e6,
                        # FP32 increment stage (stage_gauss_kernel<5, float, ..., INC>), the block's
                        # dominant kernel: 19 of the 21 launches of a 4-step block
-                       "fp32_increment": (312.3e6 + 67.1e6) / 8.0e6}
+                       "fp32_increment": (309.134336e6 + 67.868928e6) / 8.0e6}
 
 # the bench workload's config dict, identical in both arms
 CONFIG = {"workload": None, "l2": "inputs larger than L2 (three 262 MB FP64 vectors + geometry per stage)"}
