@@ -231,7 +231,11 @@ int adv_precondition(adv_solver *s, const double *src, double *dst, double mass_
 int adv_fgmres(adv_solver *s, double mass_factor, double t, const double *rhs, double *x, double rel_tol,
                int max_iterations, int *iterations, double *rel_residual, void *stream);
 /* One BDF2 step to time t_new: (3 u_new - 4 u_n + u_nm1) / (2 dt) = M^{-1} L(t_new) u_new
- * (first_step != 0: implicit Euler, u_nm1 unused), initial guess 2 u_n - u_nm1. */
+ * (first_step != 0: implicit Euler, u_nm1 unused), initial guess 2 u_n - u_nm1.
+ * Inputs and output are nodal; the linear system is solved with the vectors
+ * on the Gauss-point basis (diagonal mass matrix, no basis sweeps in the
+ * operator or the preconditioner) and stops when the nodal relative residual
+ * ||rhs - A u_new|| / ||rhs|| is at most rel_tol, as adv_fgmres does. */
 int adv_bdf2_step(adv_solver *s, double t_new, double dt, int first_step, const double *u_n, const double *u_nm1,
                   double *u_new, double rel_tol, int *iterations, void *stream);
 
