@@ -407,6 +407,20 @@ int trace_width(const adv_handle &h)
   return h.cfg.diffusion != 0.0 ? 2 : 1;
 }
 
+// Upwind traces (StageArgs::upwind_tr): each face point reads only the
+// trace of its upwind cell.  Needs the upwind flux (flux_alpha 1: one of P, M
+// is zero at every face point), a velocity constant in time (the pairs do
+// not swap between the stage that writes a trace and the one that reads
+// it), no skew term (it reads the own trace at every point), and field
+// geometry without SIPG (the kernel variant that reads traces in its passes).
+// Per cell-stage at degree 4 it saves 375 of about 4,000 FP64 instructions
+// (one contraction per pencil and direction instead of two) and 150 reads.
+bool upwind_traces(const adv_handle &h)
+{
+  return h.cfg.flux_alpha == 1.0 && h.cfg.velocity_type == ADV_VELOCITY_CONSTANT && h.cfg.factor_skew == 0.0 &&
+         !h.mesh.uniform && h.cfg.diffusion == 0.0;
+}
+
 int ensure_traces(adv_handle *h)
 {
   const size_t nb = (size_t)h->mesh.n_cells * 6 * trace_width(*h) * h->mesh.n * h->mesh.n * sizeof(double);
@@ -918,6 +932,7 @@ int plain_stage(adv_handle *h, const std::vector<double> &ai, const std::vector<
       const long long g = (long long)step * ns + st;
       A.tr_in           = h->d_traces[g & 1];
       A.tr_out          = h->d_traces[(g + 1) & 1];
+      A.upwind_tr       = upwind_traces(*h);
     }
   A.b    = bi[st] * dt * fac;
   A.a    = last ? 0.0 : ai[st] * dt * fac;
@@ -1049,7 +1064,8 @@ int increment_stage_folded(adv_handle *h, const std::vector<double> &ai, const s
               ADV_CUDA(adv::launch_face_traces(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, s, tr, 1));
               ++h->launches;
             }
-          A.tr_in = tr;
+          A.tr_in     = tr;
+          A.upwind_tr = upwind_traces(*h);
         }
       return ADV_OK;
     }

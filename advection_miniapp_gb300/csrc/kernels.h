@@ -48,7 +48,11 @@ struct StageArgs
   float         K1f[3], K2f[3], cdifff[3];
   double        adv_scale;   // velocity time factor, applied in-kernel when visc != 0
   float         adv_scalef;
-  int           pad1;
+  // face traces on field geometry without SIPG (FP64): the flux is the
+  // upwind one (at every face point one of P, M is zero) with a constant
+  // velocity and no skew term, so each face point reads only the trace of
+  // its upwind cell; stages read and write only those (see stage_gauss.cuh)
+  int           upwind_tr;
   double        mass_factor; // vmult mode: factor of the mass matrix
   float         mass_factorf;
   float         volf;        // uniform case: cell volume (det J)

@@ -74,18 +74,63 @@ struct GaussShape
   static constexpr int  GB_VALUES    = UNI || GEO_GLOBAL ? 0 : 4 * C * N * N * N;
   // viscous: Nd [C][6][NF] neighbour normal derivatives
   static constexpr int  ND_VALUES    = VISC ? 6 * C * N * N : 0;
+  // upwind traces (StageArgs::upwind_tr): per face point of the CTA's cells
+  // whether its own trace there is read, one byte each, then a count and a
+  // list of the pencils whose high trace is deferred (at most 3 C n^2)
+  static constexpr int  NEED_FLAGS   = (6 * C * N * N + 3) / 4 * 4;
+  static constexpr int  NEED_BYTES   = TG ? NEED_FLAGS + 4 * (1 + 3 * C * N * N) : 0;
   static constexpr int  SMEM         = (2 * C * N * N * N + NB_VALUES + TB_VALUES + GB_VALUES + FB_VALUES + ND_VALUES) *
-                                    (int)sizeof(T) + 12 * C * (int)sizeof(int);
+                                    (int)sizeof(T) + 12 * C * (int)sizeof(int) + NEED_BYTES;
   // byte offset of the cell geometry Gb in the layout of stage_gauss_cta
   static constexpr int GB_OFFSET = (2 * C * N * N * N + NB_VALUES + TB_VALUES) * (int)sizeof(T);
   static_assert(GB_OFFSET % 16 == 0, "cp.async destinations need 16-byte alignment");
 };
 
+__device__ __forceinline__ double or_bits(double a, double b)
+{
+  return __longlong_as_double(__double_as_longlong(a) | __double_as_longlong(b));
+}
+__device__ __forceinline__ float or_bits(float a, float b)
+{
+  return __int_as_float(__float_as_int(a) | __float_as_int(b));
+}
+// x != 0 on the integer pipe (a floating-point comparison of doubles issues
+// on the FP64 pipe, the kernel's bottleneck)
+__device__ __forceinline__ bool nonzero(double x)
+{
+  return (__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFll) != 0;
+}
+__device__ __forceinline__ bool nonzero(float x)
+{
+  return (__float_as_int(x) & 0x7FFFFFFF) != 0;
+}
+
+// Upwind traces of a pencil x: the trace at the face whose flux reads it
+// (need_lo / need_hi; the low one where neither is read), one contraction
+// with the coefficients of either face picked per thread (a pointer into
+// the tables, so a warp whose pencils need different faces runs one chain),
+// the same sum in the same order as pencil_traces.  Returns whether the
+// high trace is read as well (a diverging flow at a point of a curved cell,
+// rare): the caller defers that one.
+template <int N, typename T>
+__device__ __forceinline__ bool upwind_pencil_traces(const DevTables<T> &tb, const T (&x)[N], bool need_lo,
+                                                     bool need_hi, T *to_lo, T *to_hi)
+{
+  const bool lo = need_lo || !need_hi;
+  const T   *c  = lo ? tb.l0 : tb.l1;
+  T          s  = c[0] * x[0];
+#pragma unroll
+  for (int q = 1; q < N; ++q)
+    s = fma(c[q], x[q], s);
+  *(lo ? to_lo : to_hi) = s;
+  return need_lo && need_hi;
+}
+
 // INC: FP32 increments with the anchor's K0 folded out (StageArgs::inc32).
 // Binary32 operator: the input comes from r_in32 and the update is the
 // increment form's.  FP64 operator: the block's anchor (writes K0 and the
 // first G).
-template <int N, typename T, bool UNI, bool VISC, bool TR = false, bool INC = false>
+template <int N, typename T, bool UNI, bool VISC, bool TR = false, bool INC = false, bool UPW = false>
 __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long long cell0,
                                                 unsigned char *smem_raw)
 {
@@ -107,6 +152,9 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
   T   *Nd     = Fb + GS::FB_VALUES;              // viscous: [C][6][NF] neighbour normal derivatives
   int *s_nbr  = reinterpret_cast<int *>(Nd + GS::ND_VALUES);
   int *s_face = s_nbr + C * 6;
+  unsigned char *s_need = reinterpret_cast<unsigned char *>(s_face + C * 6); // upwind traces: [C][6][NF]
+  int *s_nboth = reinterpret_cast<int *>(s_need + GS::NEED_FLAGS);           // deferred high traces: count,
+  int *s_both  = s_nboth + 1;                                                 // [3 C NF] (d C + cl) NF + r
 
   const DevTables<T> &tb    = tab<T>(N);
   const int           tid   = threadIdx.x;
@@ -130,6 +178,8 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
                                                         128 * i));
     }
   cell_neighbours(A, cell0, ncell, s_nbr, s_face, tid, NT);
+  if (UPW && tid == 0)
+    *s_nboth = 0;
   __syncthreads();
   if (!UNI && !(GS::GEO_GLOBAL && FG))
     geometry_async<N, T>(A, cell0, ncell, s_face, Gb, Fb, tid, NT, !FG, !GS::GEO_GLOBAL);
@@ -295,6 +345,39 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
     else
       return Tb + (cl * 6 + j) * TRW * NF;
   };
+  // Upwind traces (UPW, a compile-time variant: a runtime switch between
+  // the two forms costs registers): at a face point with P = 0 or M = 0 the
+  // flux reads one side's trace, that of the upwind cell.  On a low face
+  // (flux M u_own + P u_nbr) the cell reads its own trace where M != 0 and
+  // its neighbour's where P != 0; on a high face (-(P u_own + M u_nbr)) its
+  // own where P != 0 and the neighbour's where M != 0.  Both cells of a face
+  // see the same pair, so a cell writes for the next stage exactly the
+  // traces of its own that it or its neighbour reads, and the flux is the
+  // nonzero coefficient times the value read: the same value as the general
+  // form, one product instead of a product and an FMA.
+  constexpr bool upw = UPW;
+  static_assert(!UPW || (TG && !VISC), "upwind traces are read in the passes");
+  // upwind traces at face point r of the low face j and high face j + 1 of
+  // local cell cl: the nonzero coefficient of each face and the trace on
+  // its upwind side, in the form direction_pass_pm<..., UPW> takes; returns
+  // in own_lo / own_hi whether this cell's own trace is read there (M != 0 on
+  // the low face, P != 0 on the high face), which is what the stage writes
+  using T2           = typename std::conditional<sizeof(T) == sizeof(double), double2, float2>::type;
+  auto upwind_values = [&](int cl, int j, int r, FacePM<T> &pm, T &vlo, T &vhi, bool &own_lo, bool &own_hi) {
+    const T2 pl = *reinterpret_cast<const T2 *>(faces(cl, j) + 2 * r);
+    const T2 ph = *reinterpret_cast<const T2 *>(faces(cl, j + 1) + 2 * r);
+    const T *Tr = own_tr(cl, j) + r;
+    own_lo      = nonzero(pl.y);
+    own_hi      = nonzero(ph.x);
+    // the nonzero one of P, M as the bitwise or of the two (the other is
+    // +0: 0.5 (c -+ |c|) rounds to +0), so that the compiler does not split
+    // the flux product into two predicated ones, one per side
+    pm.Plo = or_bits(pl.x, pl.y);
+    pm.Phi = or_bits(ph.x, ph.y);
+    pm.Mlo = pm.Mhi = T(0);
+    vlo             = nonzero(pl.x) ? nbv(cl, j, r) : own_lo ? trv(Tr, 0) : T(0);
+    vhi             = own_hi ? trv(Tr, TRW * NF) : nonzero(ph.y) ? nbv(cl, j + 1, r) : T(0);
+  };
 
   // ---- phase 2: x-direction terms
   for (int w = tid; w < ncell * NF; w += NT)
@@ -306,13 +389,24 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
       for (int k = 0; k < N; ++k)
         U[k] = p[k];
       const T *Tr = TR ? own_tr(cl, 0) + r : nullptr;
-      direction_pass<N, T, UNI, VISC, 0, TR>(A, tb, U, nbv(cl, 0, r), nbv(cl, 1, r),
-                                             nbd(cl, 0, r),
-                                             nbd(cl, 1, r), s_nbr[cl * 6 + 0] < 0,
-                                             s_nbr[cl * 6 + 1] < 0, r, faces(cl, 0), faces(cl, 1),
-                                             geo(cl) + N * r,
-                                             1, out, TR ? trv(Tr, 0) : T(0), TR ? trv(Tr, TRW * NF) : T(0),
-                                             TR && VISC ? trv(Tr, NF) : T(0), TR && VISC ? trv(Tr, TRW * NF + NF) : T(0));
+      if constexpr (UPW)
+        {
+          FacePM<T> pm;
+          T         vlo, vhi;
+          bool      own_lo, own_hi;
+          upwind_values(cl, 0, r, pm, vlo, vhi, own_lo, own_hi);
+          s_need[(cl * 6 + 0) * NF + r] = own_lo;
+          s_need[(cl * 6 + 1) * NF + r] = own_hi;
+          direction_pass_pm<N, T, UNI, VISC, 0, true, true>(A, tb, U, vlo, vhi, T(0), T(0), false, false, pm,
+                                                            geo(cl) + N * r, 1, out);
+        }
+      else
+        direction_pass<N, T, UNI, VISC, 0, TR>(A, tb, U, nbv(cl, 0, r), nbv(cl, 1, r), nbd(cl, 0, r),
+                                               nbd(cl, 1, r), s_nbr[cl * 6 + 0] < 0, s_nbr[cl * 6 + 1] < 0, r,
+                                               faces(cl, 0), faces(cl, 1), geo(cl) + N * r, 1, out,
+                                               TR ? trv(Tr, 0) : T(0), TR ? trv(Tr, TRW * NF) : T(0),
+                                               TR && VISC ? trv(Tr, NF) : T(0),
+                                               TR && VISC ? trv(Tr, TRW * NF + NF) : T(0));
       T *z = Qb + cl * NQ + N * r;
 #pragma unroll
       for (int k = 0; k < N; ++k)
@@ -331,13 +425,24 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
       for (int k = 0; k < N; ++k)
         U[k] = p[k * N];
       const T *Tr = TR ? own_tr(cl, 2) + r : nullptr;
-      direction_pass<N, T, UNI, VISC, 1, TR>(A, tb, U, nbv(cl, 2, r), nbv(cl, 3, r),
-                                             nbd(cl, 2, r),
-                                             nbd(cl, 3, r), s_nbr[cl * 6 + 2] < 0,
-                                             s_nbr[cl * 6 + 3] < 0, r, faces(cl, 2), faces(cl, 3),
-                                             geo(cl) + NQ + off, N, out, TR ? trv(Tr, 0) : T(0),
-                                             TR ? trv(Tr, TRW * NF) : T(0), TR && VISC ? trv(Tr, NF) : T(0),
-                                             TR && VISC ? trv(Tr, TRW * NF + NF) : T(0));
+      if constexpr (UPW)
+        {
+          FacePM<T> pm;
+          T         vlo, vhi;
+          bool      own_lo, own_hi;
+          upwind_values(cl, 2, r, pm, vlo, vhi, own_lo, own_hi);
+          s_need[(cl * 6 + 2) * NF + r] = own_lo;
+          s_need[(cl * 6 + 3) * NF + r] = own_hi;
+          direction_pass_pm<N, T, UNI, VISC, 1, true, true>(A, tb, U, vlo, vhi, T(0), T(0), false, false, pm,
+                                                            geo(cl) + NQ + off, N, out);
+        }
+      else
+        direction_pass<N, T, UNI, VISC, 1, TR>(A, tb, U, nbv(cl, 2, r), nbv(cl, 3, r), nbd(cl, 2, r),
+                                               nbd(cl, 3, r), s_nbr[cl * 6 + 2] < 0, s_nbr[cl * 6 + 3] < 0, r,
+                                               faces(cl, 2), faces(cl, 3), geo(cl) + NQ + off, N, out,
+                                               TR ? trv(Tr, 0) : T(0), TR ? trv(Tr, TRW * NF) : T(0),
+                                               TR && VISC ? trv(Tr, NF) : T(0),
+                                               TR && VISC ? trv(Tr, TRW * NF + NF) : T(0));
       T *z = Qb + cl * NQ + off;
 #pragma unroll
       for (int k = 0; k < N; ++k)
@@ -356,13 +461,23 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
       for (int k = 0; k < N; ++k)
         U[k] = p[k * NF];
       const T *G  = geo(cl);
-      const T *Tr = TR ? own_tr(cl, 4) + r : nullptr;
-      direction_pass<N, T, UNI, VISC, 2, TR>(A, tb, U, nbv(cl, 4, r), nbv(cl, 5, r),
-                                             nbd(cl, 4, r),
-                                             nbd(cl, 5, r), s_nbr[cl * 6 + 4] < 0,
-                                             s_nbr[cl * 6 + 5] < 0, r, faces(cl, 4), faces(cl, 5), G + 2 * NQ + r,
-                                             NF, out, TR ? trv(Tr, 0) : T(0), TR ? trv(Tr, TRW * NF) : T(0),
-                                             TR && VISC ? trv(Tr, NF) : T(0), TR && VISC ? trv(Tr, TRW * NF + NF) : T(0));
+      const T *Tr  = TR ? own_tr(cl, 4) + r : nullptr;
+      bool     zlo = false, zhi = false; // the z traces this pencil writes (upwind traces)
+      if constexpr (UPW)
+        {
+          FacePM<T> pm;
+          T         vlo, vhi;
+          upwind_values(cl, 4, r, pm, vlo, vhi, zlo, zhi);
+          direction_pass_pm<N, T, UNI, VISC, 2, true, true>(A, tb, U, vlo, vhi, T(0), T(0), false, false, pm,
+                                                            G + 2 * NQ + r, NF, out);
+        }
+      else
+        direction_pass<N, T, UNI, VISC, 2, TR>(A, tb, U, nbv(cl, 4, r), nbv(cl, 5, r), nbd(cl, 4, r),
+                                               nbd(cl, 5, r), s_nbr[cl * 6 + 4] < 0, s_nbr[cl * 6 + 5] < 0, r,
+                                               faces(cl, 4), faces(cl, 5), G + 2 * NQ + r, NF, out,
+                                               TR ? trv(Tr, 0) : T(0), TR ? trv(Tr, TRW * NF) : T(0),
+                                               TR && VISC ? trv(Tr, NF) : T(0),
+                                               TR && VISC ? trv(Tr, TRW * NF + NF) : T(0));
       T              *z  = Qb + cl * NQ + r;
       const long long gb = (cell0 + cl) * NQ + r;
       double          next[N]; // the next stage's input along the pencil (traces)
@@ -453,10 +568,18 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
 #pragma unroll
           for (int k = 0; k < N; ++k)
             nt[k] = from_double<T>(next[k]);
-          pencil_traces<N, T>(tb, nt, lo, hi);
-          T *to            = static_cast<T *>(A.tr_out) + ((cell0 + cl) * 6 + 4) * TRW * NF + r;
-          to[0]            = lo;
-          to[TRW * NF]     = hi;
+          T *to = static_cast<T *>(A.tr_out) + ((cell0 + cl) * 6 + 4) * TRW * NF + r;
+          if (upw)
+            {
+              if (upwind_pencil_traces<N, T>(tb, nt, zlo, zhi, to, to + TRW * NF))
+                s_both[atomicAdd(s_nboth, 1)] = (2 * C + cl) * NF + r;
+            }
+          else
+            {
+              pencil_traces<N, T>(tb, nt, lo, hi);
+              to[0]        = lo;
+              to[TRW * NF] = hi;
+            }
           if (VISC)
             {
               pencil_dtraces<N, T>(tb, nt, lo, hi);
@@ -482,15 +605,43 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
 #pragma unroll
           for (int k = 0; k < N; ++k)
             x[k] = p[k * st];
-          pencil_traces<N, T>(tb, x, lo, hi);
-          T *to        = static_cast<T *>(A.tr_out) + ((cell0 + cl) * 6 + 2 * dd) * TRW * NF + r;
-          to[0]        = lo;
-          to[TRW * NF] = hi;
+          T *to = static_cast<T *>(A.tr_out) + ((cell0 + cl) * 6 + 2 * dd) * TRW * NF + r;
+          if (upw)
+            {
+              const unsigned char *nd = s_need + (cl * 6 + 2 * dd) * NF + r;
+              if (upwind_pencil_traces<N, T>(tb, x, nd[0] != 0, nd[NF] != 0, to, to + TRW * NF))
+                s_both[atomicAdd(s_nboth, 1)] = (dd * C + cl) * NF + r;
+            }
+          else
+            {
+              pencil_traces<N, T>(tb, x, lo, hi);
+              to[0]        = lo;
+              to[TRW * NF] = hi;
+            }
           if (VISC)
             {
               pencil_dtraces<N, T>(tb, x, lo, hi);
               to[NF]            = lo;
               to[TRW * NF + NF] = hi;
+            }
+        }
+      if (upw)
+        {
+          // the deferred high traces (usually none: no thread enters the loop)
+          __syncthreads();
+          const int nb = *s_nboth;
+          for (int i = tid; i < nb; i += NT)
+            {
+              const int code = s_both[i];
+              const int dd = code / (C * NF), cl = (code / NF) % C, r = code % NF;
+              const int off = dd == 0 ? N * r : dd == 1 ? (r % N) + NF * (r / N) : r;
+              const int st  = dd == 0 ? 1 : dd == 1 ? N : NF;
+              const T  *p   = Qb + cl * NQ + off;
+              T         h   = tb.l1[0] * p[0];
+#pragma unroll
+              for (int q = 1; q < N; ++q)
+                h = fma(tb.l1[q], p[q * st], h);
+              static_cast<T *>(A.tr_out)[((cell0 + cl) * 6 + 2 * dd + 1) * TRW * NF + r] = h;
             }
         }
     }
@@ -507,39 +658,39 @@ constexpr int gauss_min_blocks()
   return TR && !UNI && !VISC && N == 5 && sizeof(T) == sizeof(double) ? 7 : 1;
 }
 
-template <int N, typename T, bool UNI, bool VISC, bool TR, bool INC>
+template <int N, typename T, bool UNI, bool VISC, bool TR, bool INC, bool UPW>
 __global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS) stage_gauss_kernel(const StageArgs A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_gauss_cta<N, T, UNI, VISC, TR, INC>(A, A.cell_begin + (long long)blockIdx.x * StageShape<N, T, UNI, VISC>::C,
-                                            smem_raw);
+  stage_gauss_cta<N, T, UNI, VISC, TR, INC, UPW>(
+    A, A.cell_begin + (long long)blockIdx.x * StageShape<N, T, UNI, VISC>::C, smem_raw);
 }
 
 // the same with the resident-CTA bound (only where gauss_min_blocks > 1: an
 // explicit bound of 1 changes the register allocation of the others)
-template <int N, typename T, bool UNI, bool VISC, bool TR, bool INC>
+template <int N, typename T, bool UNI, bool VISC, bool TR, bool INC, bool UPW>
 __global__ void __launch_bounds__(StageShape<N, T, UNI, VISC>::THREADS, (gauss_min_blocks<N, T, UNI, VISC, TR>()))
   stage_gauss_kernel_bounded(const StageArgs A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  stage_gauss_cta<N, T, UNI, VISC, TR, INC>(A, A.cell_begin + (long long)blockIdx.x * StageShape<N, T, UNI, VISC>::C,
-                                            smem_raw);
+  stage_gauss_cta<N, T, UNI, VISC, TR, INC, UPW>(
+    A, A.cell_begin + (long long)blockIdx.x * StageShape<N, T, UNI, VISC>::C, smem_raw);
 }
 
-template <int N, typename T, bool UNI, bool VISC, bool TR, bool INC>
+template <int N, typename T, bool UNI, bool VISC, bool TR, bool INC, bool UPW>
 constexpr auto gauss_kernel()
 {
   if constexpr (gauss_min_blocks<N, T, UNI, VISC, TR>() > 1)
-    return stage_gauss_kernel_bounded<N, T, UNI, VISC, TR, INC>;
+    return stage_gauss_kernel_bounded<N, T, UNI, VISC, TR, INC, UPW>;
   else
-    return stage_gauss_kernel<N, T, UNI, VISC, TR, INC>;
+    return stage_gauss_kernel<N, T, UNI, VISC, TR, INC, UPW>;
 }
 
-template <int N, typename T, bool UNI, bool VISC, bool TR, bool INC = false>
+template <int N, typename T, bool UNI, bool VISC, bool TR, bool INC = false, bool UPW = false>
 cudaError_t launch_stage_gauss_t(const StageArgs &args, cudaStream_t stream)
 {
   using GS = GaussShape<N, T, UNI, VISC, TR>;
-  constexpr auto kernel = gauss_kernel<N, T, UNI, VISC, TR, INC>();
+  constexpr auto kernel = gauss_kernel<N, T, UNI, VISC, TR, INC, UPW>();
   static std::atomic<unsigned long long> configured{0};
   cudaError_t                            e = opt_in_smem(kernel, GS::SMEM, configured);
   if (e != cudaSuccess)
@@ -559,7 +710,10 @@ cudaError_t launch_stage_gauss_n(const StageArgs &args, cudaStream_t stream)
         // the FP32-increment anchor reads traces on field geometry without
         // SIPG (and writes none)
         if (args.inc32 && !args.visc && !args.uniform)
-          return launch_stage_gauss_t<N, T, false, false, true, true>(args, stream);
+          return args.upwind_tr ? launch_stage_gauss_t<N, T, false, false, true, true, true>(args, stream)
+                                : launch_stage_gauss_t<N, T, false, false, true, true>(args, stream);
+        if (args.upwind_tr && !args.visc && !args.uniform)
+          return launch_stage_gauss_t<N, T, false, false, true, false, true>(args, stream);
         return args.visc ? launch_stage_gauss_t<N, T, false, true, true>(args, stream)
              : args.uniform ? launch_stage_gauss_t<N, T, true, false, true>(args, stream)
                             : launch_stage_gauss_t<N, T, false, false, true>(args, stream);

@@ -273,24 +273,23 @@ __device__ __forceinline__ void pencil_dtraces(const DevTables<T> &tb, const T (
 
 // OWN_TR: the own face values come precomputed (tr_lo, tr_hi), and with
 // VISC the own reference normal derivatives at the faces (dtr_lo, dtr_hi)
-template <int N, typename T, bool UNI, bool VISC, int D, bool OWN_TR = false>
-__device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTables<T> &tb,
-                                               const T (&U)[N], T nlo, T nhi, T dnlo, T dnhi, bool blo,
-                                               bool bhi, int fq, const T *Flo, const T *Fhi, const T *vt,
-                                               int vstride, T (&out)[N], T tr_lo = T(0), T tr_hi = T(0),
-                                               T dtr_lo = T(0), T dtr_hi = T(0))
+// Upwind coefficients (P, M) of the low and high face of a pencil at one
+// face point, after the exchange for a negative velocity time factor.
+template <typename T>
+struct FacePM
 {
-  constexpr int NF = N * N;
-  T             ulo, uhi;
-  if (OWN_TR)
-    ulo = tr_lo, uhi = tr_hi;
-  else
-    pencil_traces<N, T>(tb, U, ulo, uhi);
   T Plo, Mlo, Phi, Mhi;
+};
+
+// Flo / Fhi: (P, M) pairs of the low / high face (field case), read at face point fq
+template <typename T, bool UNI, int D>
+__device__ __forceinline__ FacePM<T> face_pm(const StageArgs &A, const T *Flo, const T *Fhi, int fq)
+{
+  FacePM<T> c;
   if (UNI)
     {
-      Plo = Phi = Consts<T>::P(A, D);
-      Mlo = Mhi = Consts<T>::M(A, D);
+      c.Plo = c.Phi = Consts<T>::P(A, D);
+      c.Mlo = c.Mhi = Consts<T>::M(A, D);
     }
   else
     {
@@ -298,24 +297,56 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
       using T2      = typename std::conditional<sizeof(T) == sizeof(double), double2, float2>::type;
       const T2 pmlo = *reinterpret_cast<const T2 *>(Flo + 2 * fq);
       const T2 pmhi = *reinterpret_cast<const T2 *>(Fhi + 2 * fq);
-      Plo = pmlo.x, Mlo = pmlo.y;
-      Phi = pmhi.x, Mhi = pmhi.y;
+      c.Plo = pmlo.x, c.Mlo = pmlo.y;
+      c.Phi = pmhi.x, c.Mhi = pmhi.y;
     }
   if (A.swap_pm)
     {
-      T tmp = Plo;
-      Plo   = Mlo, Mlo = tmp;
-      tmp   = Phi;
-      Phi   = Mhi, Mhi = tmp;
+      T tmp = c.Plo;
+      c.Plo = c.Mlo, c.Mlo = tmp;
+      tmp   = c.Phi;
+      c.Phi = c.Mhi, c.Mhi = tmp;
     }
+  return c;
+}
+
+// The pass with the face coefficients given (face_pm).  UPW (upwind flux,
+// one of P, M zero at every face point, no skew term): pm.Plo / pm.Phi hold
+// the nonzero coefficient of the low / high face (or zero) and nlo / nhi the
+// value on the upwind side there, own or neighbour; the flux is then one
+// product per face, with the same value as the general form.
+template <int N, typename T, bool UNI, bool VISC, int D, bool OWN_TR = false, bool UPW = false>
+__device__ __forceinline__ void direction_pass_pm(const StageArgs &A, const DevTables<T> &tb,
+                                                  const T (&U)[N], T nlo, T nhi, T dnlo, T dnhi, bool blo,
+                                                  bool bhi, const FacePM<T> &pm, const T *vt, int vstride,
+                                                  T (&out)[N], T tr_lo = T(0), T tr_hi = T(0),
+                                                  T dtr_lo = T(0), T dtr_hi = T(0))
+{
+  constexpr int NF = N * N;
+  static_assert(!UPW || (OWN_TR && !VISC), "the upwind form takes its face values from the caller");
+  T ulo, uhi;
+  if (OWN_TR)
+    ulo = tr_lo, uhi = tr_hi;
+  else
+    pencil_traces<N, T>(tb, U, ulo, uhi);
+  const T Plo = pm.Plo, Mlo = pm.Mlo, Phi = pm.Phi, Mhi = pm.Mhi;
   // numerical flux from the cell's point of view (outward normal):
   //   low face (cell is the "plus" side):  phi = M u_own + P u_nbr
   //   high face (cell is the "minus" side): phi = -P u_own - M u_nbr
   // plus the skew-symmetric correction -+ skew c u_own, c = P + M
   // (advection_solver.cc:554-574, 615-626)
-  T phlo = fma(Mlo, ulo, Plo * nlo);
-  T phhi = -fma(Phi, uhi, Mhi * nhi);
-  if (A.has_skew)
+  T phlo, phhi;
+  if constexpr (UPW)
+    {
+      phlo = Plo * nlo;
+      phhi = -(Phi * nhi);
+    }
+  else
+    {
+      phlo = fma(Mlo, ulo, Plo * nlo);
+      phhi = -fma(Phi, uhi, Mhi * nhi);
+    }
+  if (!UPW && A.has_skew)
     {
       const T sk = Consts<T>::skew(A);
       phlo       = fma(-sk * (Plo + Mlo), ulo, phlo);
@@ -458,6 +489,18 @@ __device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTabl
         }
       out[q] = o;
     }
+}
+
+template <int N, typename T, bool UNI, bool VISC, int D, bool OWN_TR = false>
+__device__ __forceinline__ void direction_pass(const StageArgs &A, const DevTables<T> &tb,
+                                               const T (&U)[N], T nlo, T nhi, T dnlo, T dnhi, bool blo,
+                                               bool bhi, int fq, const T *Flo, const T *Fhi, const T *vt,
+                                               int vstride, T (&out)[N], T tr_lo = T(0), T tr_hi = T(0),
+                                               T dtr_lo = T(0), T dtr_hi = T(0))
+{
+  direction_pass_pm<N, T, UNI, VISC, D, OWN_TR>(A, tb, U, nlo, nhi, dnlo, dnhi, blo, bhi,
+                                                face_pm<T, UNI, D>(A, Flo, Fhi, fq), vt, vstride, out, tr_lo,
+                                                tr_hi, dtr_lo, dtr_hi);
 }
 
 // Neighbour cells (-1 on boundary faces) and face ids of the cells

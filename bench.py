@@ -90,7 +90,7 @@ def _sweep_cost(n, anti):
     return inst, flops
 
 
-def fp_work_per_cell(n, curved=True, stage=True, collocation=False, traces=False):
+def fp_work_per_cell(n, curved=True, stage=True, collocation=False, traces=False, upwind=False):
     """(FP instructions, flops with FMA = 2) of one fused stage per cell,
     phase by phase as in the kernels.  Nodal form (stage_kernel.cuh):
     interpolation sweeps of the own cell (3 x n^2 pencils) and of the six
@@ -101,13 +101,18 @@ def fp_work_per_cell(n, curved=True, stage=True, collocation=False, traces=False
     sweeps; the neighbours' face values are n-term contractions at the 6 n^2
     face points.  With face traces the stage reads its own and the
     neighbours' face values and instead contracts the 3 n^2 pencils of its
-    output (2n FMAs each) for the next stage."""
+    output (2n FMAs each) for the next stage.  Upwind traces (the upwind
+    flux, where each face point reads only its upwind cell's trace): one
+    n-term contraction per pencil and direction instead of two (the rare
+    point that needs both is not counted), and one product per face flux
+    instead of a product and an FMA."""
     si, sf = _sweep_cost(n, anti=False)
     di, df = _sweep_cost(n, anti=True)
     p = n * n
     if collocation and traces:
-        inst = 3 * p * 2 * n
-        flops = 3 * p * 2 * (2 * n - 1)
+        nt = 1 if upwind else 2
+        inst = 3 * p * nt * n
+        flops = 3 * p * nt * (2 * n - 1)
     elif collocation:
         inst = 6 * p * n
         flops = 6 * p * (2 * n - 1)
@@ -118,13 +123,14 @@ def fp_work_per_cell(n, curved=True, stage=True, collocation=False, traces=False
     # per pencil and direction: 4 for the two face fluxes and 2 for their
     # sum and difference, n products vt U, the lifted even-odd sweep, n lift
     # FMAs and n additions into the accumulated Z (not in the first direction)
-    pass_i = own_i + 4 + 2 + n + di + 2 * n
+    flux_i, flux_f = (2, 2) if upwind else (4, 6)
+    pass_i = own_i + flux_i + 2 + n + di + 2 * n
     if curved and n >= 5:
         # FP64 on field geometry: the even and odd parts of vt U take one
         # product and two FMAs per mirrored pair instead of two products and
         # two additions (same flops)
         pass_i -= n // 2
-    pass_f = own_f + 6 + 2 + n + df + 4 * n
+    pass_f = own_f + flux_f + 2 + n + df + 4 * n
     inst += 3 * p * pass_i - p * n
     flops += 3 * p * pass_f - p * n
     if curved:
@@ -143,7 +149,7 @@ def fp_work_per_cell(n, curved=True, stage=True, collocation=False, traces=False
 # kernels, from ncu captures of the 40^3 curved degree-4 case (8,000,000 DoFs,
 # vectors and geometry larger than L2; profiles/ has the commands), scaled to
 # the workload by the DoF count
-NCU_TRAFFIC_PER_DOF = {"fp64": (544.2496e6 + 175.507456e6) / 8.0e6, "fp32": (297.173248e6 + 95.730432e6) / 8.0e6,
+NCU_TRAFFIC_PER_DOF = {"fp64": (531.901184e6 + 145.704960e6) / 8.0e6, "fp32": (297.173248e6 + 95.730432e6) / 8.0e6,
                        # FP32 increment stage (stage_gauss_kernel<5, float, ..., INC>), the block's
                        # dominant kernel: 19 of the 21 launches of a 4-step block
                        "fp32_increment": (309.134336e6 + 67.868928e6) / 8.0e6}
@@ -558,10 +564,11 @@ def ours(args):
     launch32 = r32["seconds"] / (STAGES * args.steps)
     # average over the 5 launches of a step: 4 stages with 2 update FMAs per DoF, the last with 1;
     # FP64 runs the collocation form, FP32 the nodal form (the library's default choice)
-    inst = (4 * fp_work_per_cell(n, collocation=True, traces=True)[0]
-            + fp_work_per_cell(n, stage=False, collocation=True, traces=True)[0]) / STAGES
-    flops = (4 * fp_work_per_cell(n, collocation=True, traces=True)[1]
-             + fp_work_per_cell(n, stage=False, collocation=True, traces=True)[1]) / STAGES
+    # (the workload's upwind flux with a constant velocity: upwind traces)
+    inst = (4 * fp_work_per_cell(n, collocation=True, traces=True, upwind=True)[0]
+            + fp_work_per_cell(n, stage=False, collocation=True, traces=True, upwind=True)[0]) / STAGES
+    flops = (4 * fp_work_per_cell(n, collocation=True, traces=True, upwind=True)[1]
+             + fp_work_per_cell(n, stage=False, collocation=True, traces=True, upwind=True)[1]) / STAGES
     flops32 = (4 * fp_work_per_cell(n)[1] + fp_work_per_cell(n, stage=False)[1]) / STAGES
     vec_bytes_launch = bytes_per_dof_step() / STAGES * n_dofs
     # FP64 instructions of any kind (FMA, add, mul) take one issue slot of the
@@ -612,7 +619,7 @@ def ours(args):
         "roofline": {"bound": "fp64", "achieved": round(achieved64, 4), "peak": round(fp64_peak, 4),
                      "unit": "TFLOP/s", "frac": round(achieved64 / fp64_peak, 4),
                      "traffic": traffic(NCU_TRAFFIC_PER_DOF["fp64"], n_dofs),
-                     "form": "collocation with face traces (Gauss-point values inside lsrk_steps)",
+                     "form": "collocation with upwind face traces (Gauss-point values inside lsrk_steps)",
                      "peak_source": "FP64 FMA microbenchmark (adv_measure_fma_peak) on this GPU",
                      "achieved_definition": "2 x FP64 instructions per second (each FP64 add/mul/FMA takes one "
                                             "FMA issue slot); algorithmic_tflops counts FMA = 2, add/mul = 1",

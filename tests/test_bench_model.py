@@ -15,6 +15,9 @@ def test_fp64_instruction_model_degree4():
     assert bench.fp_work_per_cell(5, collocation=True)[0] == 4675
     assert bench.fp_work_per_cell(5, collocation=True, traces=True)[0] == 3925
     assert bench.fp_work_per_cell(5, stage=False, collocation=True, traces=True)[0] == 3925 - 125
+    # upwind traces: one trace contraction per pencil and direction (3 x 25 x 5
+    # FMAs fewer) and one product per face flux (2 x 75 fewer)
+    assert bench.fp_work_per_cell(5, collocation=True, traces=True, upwind=True)[0] == 3925 - 375 - 150
 
 
 def test_geometry_and_increment_bytes():
