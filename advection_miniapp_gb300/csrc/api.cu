@@ -1061,7 +1061,9 @@ int increment_stage_folded(adv_handle *h, const std::vector<double> &ai, const s
           double *tr = static_cast<double *>(h->d_traces[0]);
           if (step > 0)
             {
-              ADV_CUDA(adv::launch_face_traces(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, s, tr, 1));
+              const adv::StageArgs F = base_args(*h, 0.0, 0);
+              ADV_CUDA(adv::launch_face_traces(h->mesh.n, u, h->mesh.cell_begin, h->mesh.cell_end, s, tr, 1,
+                                               upwind_traces(*h) ? &F : nullptr));
               ++h->launches;
             }
           A.tr_in     = tr;
@@ -1195,6 +1197,11 @@ int run_steps(adv_handle *h, int n_steps, int ns, bool gauss, bool traces, doubl
   const int64_t cb = h->mesh.cell_begin, ce = h->mesh.cell_end;
   const int     n  = h->mesh.n;
   double       *tr_basis = traces ? static_cast<double *>(h->d_traces[0]) : nullptr;
+  // the traces the first stage reads: only the upwind ones where it reads those
+  adv::StageArgs upw;
+  if (traces && upwind_traces(*h))
+    upw = base_args(*h, 0.0, 0);
+  const adv::StageArgs *tr_upwind = traces && upwind_traces(*h) ? &upw : nullptr;
   HostChunks    ch;
   int           nch = 0;
   if (host)
@@ -1249,7 +1256,7 @@ int run_steps(adv_handle *h, int n_steps, int ns, bool gauss, bool traces, doubl
           if (gauss)
             {
               ADV_CUDA(adv::launch_basis_change(n, u, ch.cell(ch.z[c]), ch.cell(ch.z[c + 1]), true, s, tr_basis,
-                                                trace_width(*h)));
+                                                trace_width(*h), tr_upwind));
               ++h->launches;
             }
           for (int l = ch.z[c]; l < ch.z[c + 1]; ++l)
@@ -1273,7 +1280,7 @@ int run_steps(adv_handle *h, int n_steps, int ns, bool gauss, bool traces, doubl
     }
   else if (gauss)
     {
-      ADV_CUDA(adv::launch_basis_change(n, u, cb, ce, true, s, tr_basis, trace_width(*h)));
+      ADV_CUDA(adv::launch_basis_change(n, u, cb, ce, true, s, tr_basis, trace_width(*h), tr_upwind));
       ++h->launches;
     }
   for (int step = 0; step < n_steps; ++step)

@@ -109,9 +109,12 @@ cudaError_t upload_tables_gauss32(const DevTables<double> *d, const DevTables<fl
 // to_gauss: Gauss-Lobatto nodal values -> values at the Gauss points (S x S x S);
 // otherwise the inverse (S^-1 x S^-1 x S^-1).  With traces (to_gauss only),
 // also writes the face traces of the result in the layout of StageArgs::tr_in
-// (width 2: values and reference normal derivatives, for SIPG).
+// (width 2: values and reference normal derivatives, for SIPG).  upwind
+// (width 1): only the traces an upwind-trace stage reads (StageArgs::
+// upwind_tr), with the mesh and the FP64 face coefficients of *upwind.
 cudaError_t launch_basis_change(int n, double *u, long long cell_begin, long long cell_end, bool to_gauss,
-                                cudaStream_t stream, double *traces = nullptr, int width = 1);
+                                cudaStream_t stream, double *traces = nullptr, int width = 1,
+                                const StageArgs *upwind = nullptr);
 // In-place u <- (S^T x S^T x S^T) u for the cells [cell_begin, cell_end): the
 // dual coefficients of a weak-form vector on the Gauss-point basis to those
 // on the Gauss-Lobatto nodal basis (each nodal function is the combination
@@ -122,7 +125,7 @@ cudaError_t launch_basis_dual_to_nodal(int n, double *u, long long cell_begin, l
 // values at the face points, with width 2 also the reference normal
 // derivatives), for the cells [cell_begin, cell_end); u is not changed.
 cudaError_t launch_face_traces(int n, const double *u, long long cell_begin, long long cell_end,
-                               cudaStream_t stream, double *traces, int width);
+                               cudaStream_t stream, double *traces, int width, const StageArgs *upwind = nullptr);
 // cells processed per CTA by the stage kernel (for launch accounting)
 int stage_cells_per_block(int n, int precision);
 
