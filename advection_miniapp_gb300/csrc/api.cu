@@ -413,8 +413,11 @@ int trace_width(const adv_handle &h)
 // not swap between the stage that writes a trace and the one that reads
 // it), no skew term (it reads the own trace at every point), and field
 // geometry without SIPG (the kernel variant that reads traces in its passes).
-// Per cell-stage at degree 4 it saves 375 of about 4,000 FP64 instructions
-// (one contraction per pencil and direction instead of two) and 150 reads.
+// Per cell-stage at degree 4 it saves 525 of 3,925 FP64 instructions (one
+// trace contraction per pencil and direction instead of two, one product
+// per face flux instead of two instructions) and 150 trace reads; measured
+// on GB300 on 64^3 curved cells of degree 4: 1.717 instead of 2.107 ms per
+// stage launch.
 bool upwind_traces(const adv_handle &h)
 {
   return h.cfg.flux_alpha == 1.0 && h.cfg.velocity_type == ADV_VELOCITY_CONSTANT && h.cfg.factor_skew == 0.0 &&
