@@ -237,66 +237,77 @@ __device__ __forceinline__ void stage_gauss_cta(const StageArgs &A, const long l
           Tb[i] = __ldg(tr + i);
       }
   }
-  for (int w = tid; w < (TG ? 0 : ncell * 6 * NF); w += NT)
+  // the neighbours' values at the face points: one thread per face point
+  // position (cell, fq), the six faces unrolled (face, direction, stride and
+  // basis known at compile time)
+  auto neighbour_value = [&](int cl, int j, int fq) {
+    const int cf = cl * 6 + j, d = j >> 1;
+    const int nb = s_nbr[cf];
+    if (nb >= 0)
+      {
+        if (TR)
+          {
+            // the neighbour's own trace on the shared face (its face j ^ 1)
+            const T *tn      = static_cast<const T *>(A.tr_in) + ((long long)nb * 6 + (j ^ 1)) * TRW * NF + fq;
+            Nb[cf * NF + fq] = __ldg(tn);
+            if (VISC)
+              Nd[cf * NF + fq] = __ldg(tn + NF);
+            return;
+          }
+        // pencil of the neighbour along d through face point fq, contracted
+        // with its basis at the shared face: xi_d = 1 for the neighbour
+        // below (low face, j even), xi_d = 0 for the one above
+        const T        *l   = (j & 1) ? tb.l0 : tb.l1;
+        const int       sd  = d == 0 ? 1 : d == 1 ? N : NF;
+        const long long off = (long long)nb * NQ + idx3<N>(d, 0, fq % N, fq / N);
+        T               v[N];
+        if (INC && sizeof(T) == sizeof(float))
+          {
+#pragma unroll
+            for (int a = 0; a < N; ++a)
+              v[a] = T(__ldg(A.r_in32 + off + a * sd));
+          }
+        else
+          {
+#pragma unroll
+            for (int a = 0; a < N; ++a)
+              v[a] = from_double<T>(__ldg(A.r_in + off + a * sd));
+          }
+        T s = l[0] * v[0];
+#pragma unroll
+        for (int a = 1; a < N; ++a)
+          s = fma(l[a], v[a], s);
+        Nb[cf * NF + fq] = s;
+        if (VISC)
+          {
+            const T *ld = (j & 1) ? tb.ld0 : tb.ld1;
+            T        ds = ld[0] * v[0];
+#pragma unroll
+            for (int a = 1; a < N; ++a)
+              ds = fma(ld[a], v[a], ds);
+            Nd[cf * NF + fq] = ds;
+          }
+      }
+    else
+      {
+        double g = 0.0;
+        if (A.bc_exact)
+          {
+            const double *fx = d == 0 ? A.face_x[0] : d == 1 ? A.face_x[1] : A.face_x[2];
+            const double *x  = fx + ((size_t)s_face[cf] * NF + fq) * 3;
+            g                = exact_value(A.ex, x[0], x[1], x[2], A.t);
+          }
+        Nb[cf * NF + fq] = from_double<T>(g);
+      }
+  };
+  for (int w = tid; w < (TG ? 0 : ncell * NF); w += NT)
     {
-      const int cf = w / NF, fq = w % NF;
-      const int j = cf % 6, d = j >> 1;
-      const int nb = s_nbr[cf];
-      if (nb >= 0)
+      const int cl = w / NF, fq = w % NF;
+#pragma unroll 1
+      for (int d = 0; d < 3; ++d)
         {
-          if (TR)
-            {
-              // the neighbour's own trace on the shared face (its face j ^ 1)
-              const T *tn      = static_cast<const T *>(A.tr_in) + ((long long)nb * 6 + (j ^ 1)) * TRW * NF + fq;
-              Nb[cf * NF + fq] = __ldg(tn);
-              if (VISC)
-                Nd[cf * NF + fq] = __ldg(tn + NF);
-              continue;
-            }
-          // pencil of the neighbour along d through face point fq, contracted
-          // with its basis at the shared face: xi_d = 1 for the neighbour
-          // below (low face, j even), xi_d = 0 for the one above
-          const T      *l  = (j & 1) ? tb.l0 : tb.l1;
-          const int       sd  = d == 0 ? 1 : d == 1 ? N : NF;
-          const long long off = (long long)nb * NQ + idx3<N>(d, 0, fq % N, fq / N);
-          T               v[N];
-          if (INC && sizeof(T) == sizeof(float))
-            {
-#pragma unroll
-              for (int a = 0; a < N; ++a)
-                v[a] = T(__ldg(A.r_in32 + off + a * sd));
-            }
-          else
-            {
-#pragma unroll
-              for (int a = 0; a < N; ++a)
-                v[a] = from_double<T>(__ldg(A.r_in + off + a * sd));
-            }
-          T s = l[0] * v[0];
-#pragma unroll
-          for (int a = 1; a < N; ++a)
-            s = fma(l[a], v[a], s);
-          Nb[cf * NF + fq] = s;
-          if (VISC)
-            {
-              const T *ld = (j & 1) ? tb.ld0 : tb.ld1;
-              T        ds = ld[0] * v[0];
-#pragma unroll
-              for (int a = 1; a < N; ++a)
-                ds = fma(ld[a], v[a], ds);
-              Nd[cf * NF + fq] = ds;
-            }
-        }
-      else
-        {
-          double g = 0.0;
-          if (A.bc_exact)
-            {
-              const double *fx = d == 0 ? A.face_x[0] : d == 1 ? A.face_x[1] : A.face_x[2];
-              const double *x  = fx + ((size_t)s_face[cf] * NF + fq) * 3;
-              g                = exact_value(A.ex, x[0], x[1], x[2], A.t);
-            }
-          Nb[cf * NF + fq] = from_double<T>(g);
+          neighbour_value(cl, 2 * d, fq);
+          neighbour_value(cl, 2 * d + 1, fq);
         }
     }
   if (!UNI)

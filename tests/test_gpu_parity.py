@@ -45,6 +45,13 @@ CASES = {
                               ic_params=(0.5, 0.5, 0.5, 0.15), mesh_type=1, deformation=0.05),
     "sipg-exact-bc-k5-skew": dict(degree=5, n_cells=(2, 2, 3), periodic=0, diffusion=1e-3, factor_skew=0.5,
                                   initial_condition=2, boundary_value=1),
+    # curved cells where the FP64 stages read every face trace (the upwind
+    # traces need the upwind flux, a constant velocity and no skew term)
+    "curved-k3-lax-friedrichs": dict(degree=3, n_cells=(3, 3, 2), mesh_type=1, deformation=0.07, flux_alpha=0.5),
+    "curved-k4-skew": dict(degree=4, n_cells=(2, 3, 2), mesh_type=1, deformation=0.05, factor_skew=0.3),
+    "curved-rotating-k3": dict(degree=3, n_cells=(3, 2, 3), mesh_type=1, deformation=0.05, periodic=0,
+                               velocity_type=1, velocity=(1.0, 1.0, 0.3), velocity_period=0.5, initial_condition=1,
+                               ic_params=(0.3, 0.5, 0.5, 0.1), boundary_value=0),
 }
 
 
