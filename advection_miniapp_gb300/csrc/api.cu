@@ -1548,7 +1548,7 @@ int adv_fdm_tables(int degree, double flux_alpha, int sign_index, double *lambda
 
 int adv_measure_fma_peak(int precision, double *tflops, void *stream)
 {
-  if (!tflops || (precision != 0 && precision != 1))
+  if (!tflops || precision < 0 || precision > 2)
     return fail(ADV_ERR_INVALID, "bad argument");
   cudaStream_t s   = (cudaStream_t)stream;
   int          dev = 0, sms = 0;
@@ -1557,7 +1557,7 @@ int adv_measure_fma_peak(int precision, double *tflops, void *stream)
   const int blocks = sms * 8;
   double   *buf    = nullptr;
   ADV_CUDA(cudaMalloc(&buf, (size_t)blocks * 256 * sizeof(double)));
-  const int   iters = precision == 0 ? 4096 : 65536;
+  const int   iters = precision == 1 ? 65536 : 4096;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -1584,7 +1584,9 @@ int adv_measure_fma_peak(int precision, double *tflops, void *stream)
   cudaFree(buf);
   if (rc)
     return rc;
-  *tflops = 2.0 * 8.0 * iters * (double)blocks * 256 / (best * 1e-3) / 1e12;
+  // FMA-equivalent TFLOP/s: 2 x instructions per second (8 chains per
+  // iteration, 13 for the FP64 mix)
+  *tflops = 2.0 * (precision == 2 ? 13.0 : 8.0) * iters * (double)blocks * 256 / (best * 1e-3) / 1e12;
   return ADV_OK;
 }
 

@@ -319,8 +319,10 @@ int adv_fdm_tables(int degree, double flux_alpha, int sign_index, double *lambda
 /* Number of kernel launches the library has issued on this handle. */
 int adv_launch_count(const adv_handle *h, int64_t *out);
 
-/* Measured FP64 / FP32 fused multiply-add throughput of the current device in
- * TFLOP/s (FMA = 2 flops), for roofline denominators.  Synchronises. */
+/* Measured FP64 (precision 0) / FP32 (1) fused multiply-add throughput of the
+ * current device in TFLOP/s (FMA = 2 flops), for roofline denominators; 2:
+ * FP64 instructions in the stage kernels' mix of FMA, MUL and ADD (6 : 3 : 4),
+ * as 2 x instructions per second.  Synchronises. */
 int adv_measure_fma_peak(int precision, double *tflops, void *stream);
 
 /* No counterpart in the reference.  adv_perform_stage for callers that must
