@@ -1584,9 +1584,8 @@ int adv_measure_fma_peak(int precision, double *tflops, void *stream)
   cudaFree(buf);
   if (rc)
     return rc;
-  // FMA-equivalent TFLOP/s: 2 x instructions per second (8 chains per
-  // iteration, 13 for the FP64 mix)
-  *tflops = 2.0 * (precision == 2 ? 13.0 : 8.0) * iters * (double)blocks * 256 / (best * 1e-3) / 1e12;
+  // FMA-equivalent TFLOP/s: 2 x instructions per second
+  *tflops = 2.0 * adv::fma_peak_chains(precision) * iters * (double)blocks * 256 / (best * 1e-3) / 1e12;
   return ADV_OK;
 }
 

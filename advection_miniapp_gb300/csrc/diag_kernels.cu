@@ -373,43 +373,43 @@ __global__ void fma_peak_kernel(T *out, int iters, T a, T b)
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
-// FP64 with the stage kernels' mix of FP64 instructions: per iteration 13
-// independent chains, 6 FMA, 3 MUL and 4 ADD (the collocation stage with
-// upwind traces issues about 51 % FMA, 28 % MUL and 21 % ADD, the changes of
-// basis 46 / 23 / 31 %)
+// FP64 with the stage kernel's mix of FP64 instructions: per iteration 14
+// independent chains, 7 FMA, 4 MUL and 3 ADD (the collocation stage with
+// upwind traces issues about 51 % FMA, 28 % MUL and 21 % ADD)
+constexpr int kMixF = 7, kMixM = 4, kMixA = 3;
 __global__ void fp64_mix_kernel(double *out, int iters, double a, double b)
 {
-  double f[6], m[3], d[4];
+  double f[kMixF], m[kMixM], d[kMixA];
 #pragma unroll
-  for (int i = 0; i < 6; ++i)
+  for (int i = 0; i < kMixF; ++i)
     f[i] = threadIdx.x + i;
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
-    m[i] = threadIdx.x + 6 + i;
+  for (int i = 0; i < kMixM; ++i)
+    m[i] = threadIdx.x + kMixF + i;
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
-    d[i] = threadIdx.x + 9 + i;
+  for (int i = 0; i < kMixA; ++i)
+    d[i] = threadIdx.x + kMixF + kMixM + i;
   for (int it = 0; it < iters; ++it)
     {
 #pragma unroll
-      for (int i = 0; i < 6; ++i)
+      for (int i = 0; i < kMixF; ++i)
         f[i] = fma(f[i], a, b);
 #pragma unroll
-      for (int i = 0; i < 3; ++i)
+      for (int i = 0; i < kMixM; ++i)
         m[i] = m[i] * a;
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < kMixA; ++i)
         d[i] = d[i] + b;
     }
   double s = 0.0;
 #pragma unroll
-  for (int i = 0; i < 6; ++i)
+  for (int i = 0; i < kMixF; ++i)
     s += f[i];
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+  for (int i = 0; i < kMixM; ++i)
     s += m[i];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < kMixA; ++i)
     s += d[i];
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
@@ -464,6 +464,11 @@ cudaError_t launch_l2_error(const DiagArgs &g, const double *u, double t, double
 }
 
 // out must hold blocks * 256 values of the precision's type
+int fma_peak_chains(int precision)
+{
+  return precision == 2 ? kMixF + kMixM + kMixA : 8;
+}
+
 cudaError_t launch_fma_peak(int precision, double *out, int iters, int blocks, cudaStream_t s)
 {
   if (precision == 2)

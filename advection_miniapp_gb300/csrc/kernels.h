@@ -170,4 +170,6 @@ cudaError_t launch_l2_error(const DiagArgs &g, const double *u, double t, double
                             int *n_blocks, cudaStream_t s);
 int diag_max_blocks(long long n_cells);
 cudaError_t launch_fma_peak(int precision, double *out, int iters, int blocks, cudaStream_t s);
+// independent chains per loop iteration of that microbenchmark
+int fma_peak_chains(int precision);
 } // namespace adv

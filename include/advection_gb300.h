@@ -321,7 +321,7 @@ int adv_launch_count(const adv_handle *h, int64_t *out);
 
 /* Measured FP64 (precision 0) / FP32 (1) fused multiply-add throughput of the
  * current device in TFLOP/s (FMA = 2 flops), for roofline denominators; 2:
- * FP64 instructions in the stage kernels' mix of FMA, MUL and ADD (6 : 3 : 4),
+ * FP64 instructions in the stage kernel's mix of FMA, MUL and ADD (7 : 4 : 3),
  * as 2 x instructions per second.  Synchronises. */
 int adv_measure_fma_peak(int precision, double *tflops, void *stream);
 
